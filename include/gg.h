@@ -1,0 +1,198 @@
+/*
+ * gg.h -- C ABI of the GB300 convolutional gridder (libgg.so).
+ *
+ * Plain pointers and sizes only.  Every function returns a status code
+ * (GG_OK = 0); gg_last_error() gives the message of the last failure on the
+ * calling thread.
+ *
+ * Reference interfaces replaced (paths within NVIDIA/SKA-gpu-grid):
+ *   gridGPU<CmplxOutType,CmplxType>   grid_gpu.cuh:30-32, grid_gpu.cu:675-819,
+ *                                     instantiations grid_gpu.cu:820-825
+ *   vis2ints                          grid_gpu.cu:352-365
+ *   set_bookmarks                     grid_gpu.cu:366-390
+ *   Defines.h compile-time switches   Defines.h:57-77, Makefile:30-60
+ *   GPUGrid.convgrid (Python 2)       GPUGrid.cpp:124-164
+ *
+ * Coordinates are in grid pixels (the caller centres them, as in grid.cu:446).
+ * Taps of a visibility at main cell m cover m-S/2+1 .. m+S/2 on each axis
+ * (grid.cu:167-168); taps outside [0, img_dim) are dropped.  The GCF table is
+ * [G*G][S][S] complex, indexed [sub_y*G+sub_x][b'][a'] with a'=a+S/2-1.
+ */
+#ifndef GG_H
+#define GG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GG_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define GG_OK 0
+#define GG_ERR_ARG 1      /* invalid argument or unsupported combination     */
+#define GG_ERR_CUDA 2     /* a CUDA runtime call failed                      */
+#define GG_ERR_NOMEM 3    /* device or pinned-host allocation failed         */
+#define GG_ERR_UNSORTED 4 /* input declared tile-sorted is not               */
+#define GG_ERR_BUDGET 5   /* request larger than the server's HBM budget     */
+#define GG_ERR_TIMEOUT 6  /* a bounded device or host wait expired           */
+#define GG_ERR_CANCELLED 7
+#define GG_ERR_STATE 8    /* object used after failure / in the wrong state  */
+
+/* ---- element types ----------------------------------------------------- */
+#define GG_C64 0  /* float2:  complex64,  or (u,v) as two floats             */
+#define GG_C128 1 /* double2: complex128, or (u,v) as two doubles            */
+
+/* ---- gridding method: the reference's compile-time GATHER= / MOVING_WINDOW=
+ *      switches (Makefile:37-45) become a run-time field ------------------ */
+#define GG_MODE_SCATTER 0 /* per-tap native red.global adds                  */
+#define GG_MODE_GATHER 1  /* one output cell per thread over uv-tile bins    */
+#define GG_MODE_WINDOW 2  /* register + shared-memory moving window per tile */
+#define GG_MODE_AUTO 3    /* autotuner's choice for the size class           */
+
+/* ---- output layout ----------------------------------------------------- */
+#define GG_LAYOUT_INTERLEAVED 0 /* P planes of N*N (re,im) pairs             */
+#define GG_LAYOUT_PLANAR 1      /* re[P][N][N] then im[P][N][N] (gridCPU_pz) */
+#define GG_LAYOUT_REFERENCE 2   /* what gridGPU writes per method: planar for
+                                   the moving window (grid_gpu.cu:524-525),
+                                   interleaved otherwise (:162-163, :500)   */
+
+/* ---- accumulation ------------------------------------------------------ */
+#define GG_ACC_PLAIN 0       /* arithmetic in the values' precision         */
+#define GG_ACC_COMPENSATED 1 /* FP32 two-sum hi/lo per cell (FP32 values)    */
+
+/* ---- GCF source -------------------------------------------------------- */
+#define GG_GCF_TABLE 0    /* tabulated [G*G][S][S] complex (init_gcf layout)  */
+#define GG_GCF_GAUSSIAN 1 /* COMPUTE_GCF: separable exp(-x^2/(2 sigma^2)),
+                             x = a - sub/G, evaluated on the device          */
+#define GG_GCF_COUNT 2    /* DEBUG1 footprint mode (Defines.h:78): every tap
+                             adds (1, visibility index)                     */
+
+typedef struct gg_options {
+  int32_t mode;          /* GG_MODE_*                                        */
+  int32_t layout;        /* GG_LAYOUT_*                                      */
+  int32_t accum;         /* GG_ACC_*                                         */
+  int32_t gcf_kind;      /* GG_GCF_*                                         */
+  int32_t oversample;    /* GCF_GRID: power of two, 1..64 (default 8)        */
+  int32_t polarizations; /* POLARIZATIONS: 1..8 (default 1)                  */
+  int32_t tile;          /* uv tile side in cells for binning (default 32)   */
+  int32_t input_sorted;  /* 1: caller guarantees visibilities are grouped by
+                            uv tile in ascending tile id (checked)            */
+  double gcf_sigma;      /* GG_GCF_GAUSSIAN: sigma in cells; 0 -> S/4        */
+  int32_t window_chunk;  /* max visibilities per work item (0 -> default)    */
+  int32_t reserved[7];
+} gg_options;
+
+/* Defaults = the reference built with no Makefile switches: SCATTER,
+ * REFERENCE layout, PLAIN, TABLE, G=8, P=1; tile 32. */
+int gg_default_options(gg_options *opt);
+
+/* Process-wide options used by the drop-in gridGPU entry points below, the
+ * run-time counterpart of Defines.h / Makefile switches. */
+int gg_set_global_options(const gg_options *opt);
+int gg_get_global_options(gg_options *opt);
+
+const char *gg_last_error(void);
+int gg_abi_version(void);
+
+/* ---- drop-in gridGPU: HOST buffers, reference semantics ----------------
+ * out: (img_dim^2 + 2*img_dim*gcf_dim + 2*gcf_dim) * P elements; the grid is
+ * written at element offset img_dim*gcf_dim + gcf_dim and everything else is
+ * zeroed, i.e. out is overwritten, never accumulated (grid_gpu.cu:755-800).
+ * in: npts (u,v); in_vals: npts*P complex; gcf: G*G*S*S complex, un-offset.
+ * Unlike the reference these allocate nothing per call (a context owns the
+ * device buffers), pin nothing, and report errors.                          */
+int gg_gridGPU_zz(double *out, const double *in, const double *in_vals,
+                  size_t npts, size_t img_dim, const double *gcf,
+                  size_t gcf_dim); /* gridGPU<double2,double2> */
+int gg_gridGPU_zc(double *out, const float *in, const float *in_vals,
+                  size_t npts, size_t img_dim, const float *gcf,
+                  size_t gcf_dim); /* gridGPU<double2,float2>  */
+int gg_gridGPU_cc(float *out, const float *in, const float *in_vals,
+                  size_t npts, size_t img_dim, const float *gcf,
+                  size_t gcf_dim); /* gridGPU<float2,float2>   */
+
+/* The same with explicit options and element types (uv_type and vals_type
+ * may differ, e.g. FP64 coordinates with complex64 values). */
+int gg_grid_host(const gg_options *opt, int out_type, void *out, int uv_type,
+                 const void *uv, int vals_type, const void *vals, size_t npts,
+                 size_t img_dim, const void *gcf, size_t gcf_dim);
+
+/* ---- device-resident API ------------------------------------------------ */
+typedef struct gg_context gg_context;
+
+int gg_create(gg_context **ctx, int device);
+int gg_destroy(gg_context *ctx);
+/* Pre-size the context's device workspace for jobs up to these sizes so that
+ * later calls allocate nothing (needed before CUDA-graph capture). */
+int gg_reserve(gg_context *ctx, const gg_options *opt, int64_t max_npts,
+               int64_t max_img_dim, int64_t max_gcf_dim, int32_t vals_type);
+/* bytes of device workspace the context holds */
+int gg_workspace_bytes(gg_context *ctx, size_t *bytes);
+
+typedef struct gg_job {
+  void *out;          /* device grid head: N*N*P complex of out_type; it is
+                         overwritten (zeroed first) by the call            */
+  const void *uv;     /* device: npts (u,v) pairs of uv_type              */
+  const void *vals;   /* device: npts*P complex of vals_type              */
+  const void *gcf;    /* device: G*G*S*S complex of vals_type (TABLE)     */
+  int64_t npts;
+  int64_t img_dim;
+  int64_t gcf_dim;
+  int32_t uv_type, vals_type, out_type;
+  int32_t reserved0;
+  double gcf_sigma;   /* overrides options.gcf_sigma when > 0             */
+  int64_t reserved[4];
+} gg_job;
+
+/* Grid one job on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream).  Asynchronous: returns after enqueueing. */
+int gg_grid_device(gg_context *ctx, const gg_options *opt, const gg_job *job,
+                   void *stream);
+
+/* Many independent jobs in one persistent launch over a device work queue of
+ * (job, uv tile) items.  All jobs share opt, S-class and types. */
+int gg_grid_batch(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
+                  int32_t njobs, void *stream);
+
+/* Counters of the last completed calls on this context (synchronises the
+ * stream): [0] visibilities dropped because their oversample index fell
+ * outside [0,G) (u not float-representable right below an integer),
+ * [1] bounded-wait timeouts, [2] unsorted input detected. */
+int gg_read_flags(gg_context *ctx, void *stream, int32_t flags[4]);
+
+/* Profiling (the reference's getElapsed event timer, grid_gpu.cu:38-44, made
+ * per phase): when enabled, every grid call records CUDA events on its own
+ * stream around the binning pass and around the gridding kernels. */
+int gg_profile_enable(gg_context *ctx, int on);
+/* Times in ms of the last grid call on ctx: [0] binning (index step, tile
+ * sort, bookmarks, work queue), [1] gridding kernels, [2] whole call.
+ * Waits for that call's last event. */
+int gg_profile_last(gg_context *ctx, double ms[3]);
+/* Kernels launched by this process through libgg so far. */
+int gg_kernel_launches(int64_t *count);
+
+/* vis2ints (grid_gpu.cu:352-365) on device buffers: packed[2n] = main_x*G +
+ * sub_x, packed[2n+1] = main_y*G + sub_y, bit-exact with grid.cu:159-163. */
+int gg_vis2ints(int uv_type, const void *uv, int64_t npts, int32_t oversample,
+                int32_t *packed, void *stream);
+
+/* Bin visibilities by uv tile of `tile` cells (the device replacement of the
+ * reference's host sorts, grid.cu:467-475, and set_bookmarks).  On return
+ * (device buffers):
+ *   bookmarks[z] = first sorted position of tile z, z in [0, ntiles]
+ *                  (ntiles = ceil(img_dim/tile)^2; set_bookmarks semantics)
+ *   order[k]     = input index of the visibility at sorted position k
+ * Visibilities whose footprint misses the grid are left out: bookmarks[ntiles]
+ * is the number kept.  Within a tile, input order is kept when
+ * opt->input_sorted is set; otherwise it is unspecified. */
+int gg_bin(gg_context *ctx, const gg_options *opt, int uv_type, const void *uv,
+           int64_t npts, int64_t img_dim, int64_t gcf_dim, int32_t *bookmarks,
+           int32_t *order, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GG_H */

@@ -1,0 +1,193 @@
+/*
+ * CPU oracle for the convolutional gridder -- TEST INFRASTRUCTURE ONLY.
+ * See grid_oracle.h.  Compiled with -ffp-contract=off so that every
+ * a*b-c*d is two rounded products and one rounded difference, as the
+ * reference's x86 build computes it (an aarch64 compiler would otherwise
+ * fuse them into FMAs).
+ */
+#include "grid_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* The index step of gridCPU_pz, grid.cu:159-163.  floorf() receives a double
+ * argument there, so C converts it to float first; GCF_GRID*(...) is then
+ * evaluated in double and converted to float again by the outer floorf. */
+static inline void index_step(double u, int G, int *main_i, int *sub_i) {
+  float uf = (float)u;
+  double frac = (double)G * (u - (double)floorf(uf));
+  *sub_i = (int)floorf((float)frac);
+  *main_i = (int)floor(u);
+}
+
+typedef struct {
+  double *out;
+  const double *uv, *vals, *gcf;
+  size_t npts, img_dim, gcf_dim;
+  int G, P, debug1;
+  long y0, y1; /* rows owned by this worker: [y0, y1) */
+} band_job;
+
+/* Body of gridCPU_pz (grid.cu:157-191), restricted to rows [y0, y1).  The
+ * tap loops run a (then b) from S/2 down to -S/2+1 (grid.cu:167-168); each
+ * cell receives at most one addition per visibility, so the order of
+ * additions into any one cell is the visibility order n. */
+static void grid_band(const band_job *j) {
+  const long S = (long)j->gcf_dim, N = (long)j->img_dim;
+  const int G = j->G, P = j->P;
+  /* gcf += GCF_DIM*(GCF_DIM-1)/2-1 (grid.cu:152), in complex elements */
+  const double *gcf = j->gcf + 2 * (S * (S - 1) / 2 - 1);
+  double *out1 = j->out;
+  double *out2 = j->out + (size_t)P * N * N; /* grid.cu:154 */
+  for (size_t n = 0; n < j->npts; n++) {
+    int main_x, main_y, sub_x, sub_y;
+    index_step(j->uv[2 * n], G, &main_x, &sub_x);
+    index_step(j->uv[2 * n + 1], G, &main_y, &sub_y);
+    if ((long)main_y + S / 2 < j->y0 || (long)main_y - S / 2 + 1 >= j->y1)
+      continue; /* footprint misses this band entirely */
+    const double *g = gcf + 2 * (S * S * ((long)G * sub_y + sub_x));
+    for (long a = S / 2; a > -S / 2; a--)
+      for (long b = S / 2; b > -S / 2; b--) {
+        long x = main_x + a, y = main_y + b;
+        if (x < 0 || y < 0 || x >= N || y >= N) continue;
+        if (y < j->y0 || y >= j->y1) continue;
+        double r2 = g[2 * (S * b + a)], i2 = g[2 * (S * b + a) + 1];
+        for (int p = 0; p < P; p++) {
+          size_t cell = (size_t)x + (size_t)N * y + (size_t)p * N * N;
+          if (j->debug1) {
+            out1[cell] += 1;
+            out2[cell] += (double)n;
+          } else {
+            double r1 = j->vals[2 * (P * n + p)];
+            double i1 = j->vals[2 * (P * n + p) + 1];
+            out1[cell] += r1 * r2 - i1 * i2;
+            out2[cell] += r1 * i2 + r2 * i1;
+          }
+        }
+      }
+  }
+}
+
+void oracle_grid_pz(double *out_planar, const double *uv, const double *vals,
+                    size_t npts, size_t img_dim, const double *gcf,
+                    size_t gcf_dim, int gcf_grid, int pols, int debug1) {
+  band_job j = {out_planar, uv, vals, gcf, npts, img_dim, gcf_dim,
+                gcf_grid, pols, debug1, 0, (long)img_dim};
+  grid_band(&j);
+}
+
+static void *band_thread(void *arg) {
+  grid_band((const band_job *)arg);
+  return NULL;
+}
+
+void oracle_grid_pz_mt(double *out_planar, const double *uv,
+                       const double *vals, size_t npts, size_t img_dim,
+                       const double *gcf, size_t gcf_dim, int gcf_grid,
+                       int pols, int debug1, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if ((size_t)nthreads > img_dim) nthreads = (int)img_dim;
+  band_job *jobs = (band_job *)calloc((size_t)nthreads, sizeof(band_job));
+  pthread_t *tid = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+  for (int t = 0; t < nthreads; t++) {
+    band_job j = {out_planar, uv, vals, gcf, npts, img_dim, gcf_dim,
+                  gcf_grid, pols, debug1,
+                  (long)(img_dim * (size_t)t / (size_t)nthreads),
+                  (long)(img_dim * (size_t)(t + 1) / (size_t)nthreads)};
+    jobs[t] = j;
+  }
+  char *joined = (char *)calloc((size_t)nthreads, 1);
+  for (int t = 1; t < nthreads; t++)
+    if (pthread_create(&tid[t], NULL, band_thread, &jobs[t]) == 0)
+      joined[t] = 1;
+    else
+      grid_band(&jobs[t]); /* no thread: do the band here */
+  grid_band(&jobs[0]);
+  for (int t = 1; t < nthreads; t++)
+    if (joined[t]) pthread_join(tid[t], NULL);
+  free(joined);
+  free(jobs);
+  free(tid);
+}
+
+void oracle_vis2ints(const double *uv, size_t npts, int gcf_grid,
+                     int32_t *packed_xy) {
+  for (size_t n = 0; n < npts; n++) {
+    int mx, sx, my, sy;
+    index_step(uv[2 * n], gcf_grid, &mx, &sx);
+    index_step(uv[2 * n + 1], gcf_grid, &my, &sy);
+    packed_xy[2 * n] = mx * gcf_grid + sx;
+    packed_xy[2 * n + 1] = my * gcf_grid + sy;
+  }
+}
+
+void oracle_vis2ints_gpu_formula(const double *uv, size_t npts, int gcf_grid,
+                                 int32_t *packed_xy) {
+  for (size_t n = 0; n < npts; n++) {
+    /* grid_gpu.cu:358-363: main = floor(v) (to int), sub = floor(G*(v-main))
+     * with the int main promoted back to double */
+    int my = (int)floor(uv[2 * n + 1]);
+    int sy = (int)floor(gcf_grid * (uv[2 * n + 1] - my));
+    int mx = (int)floor(uv[2 * n]);
+    int sx = (int)floor(gcf_grid * (uv[2 * n] - mx));
+    packed_xy[2 * n] = mx * gcf_grid + sx;
+    packed_xy[2 * n + 1] = my * gcf_grid + sy;
+  }
+}
+
+void oracle_set_bookmarks(const int32_t *packed_xy, size_t npts, int gcf_grid,
+                          int blocksize, int blockgrid, int32_t *bookmarks) {
+  /* grid_gpu.cu:369-389, run serially over q = 0..npts.  The reference's
+   * final step fills up to blockgrid*blockgrid + blockgrid; the restatement
+   * stops at the last meaningful entry, ntiles = blockgrid^2. */
+  const long ntiles = (long)blockgrid * blockgrid;
+  for (size_t q = 0; q <= npts; q++) {
+    int mx, my, mxl, myl;
+    if (q == 0) {
+      myl = 0;
+      mxl = -1;
+    } else {
+      /* C integer division, as in the reference (truncates toward zero) */
+      mxl = packed_xy[2 * (q - 1)] / gcf_grid / blocksize;
+      myl = packed_xy[2 * (q - 1) + 1] / gcf_grid / blocksize;
+    }
+    if (q == npts) {
+      mx = my = blockgrid;
+    } else {
+      mx = packed_xy[2 * q] / gcf_grid / blocksize;
+      my = packed_xy[2 * q + 1] / gcf_grid / blocksize;
+    }
+    if (mx != mxl || my != myl) {
+      for (long z = (long)myl * blockgrid + mxl + 1;
+           z <= (long)my * blockgrid + mx && z <= ntiles; z++)
+        bookmarks[z] = (int32_t)q;
+    }
+  }
+}
+
+void oracle_gcf_from_1d(double *gcf, const double *g1, int S, int G) {
+  for (int sy = 0; sy < G; sy++)
+    for (int sx = 0; sx < G; sx++)
+      for (int bp = 0; bp < S; bp++)
+        for (int ap = 0; ap < S; ap++) {
+          size_t k = (size_t)S * S * (sy * G + sx) + (size_t)S * bp + ap;
+          gcf[2 * k] = g1[sx * S + ap] * g1[sy * S + bp];
+          gcf[2 * k + 1] = 0.0;
+        }
+}
+
+void oracle_gaussian_gcf(double *gcf, double *g1, int S, int G,
+                         double sigma) {
+  double *g = g1 ? g1 : (double *)malloc(sizeof(double) * S * G);
+  for (int s = 0; s < G; s++)
+    for (int ap = 0; ap < S; ap++) {
+      /* tap a = a'-S/2+1 lands on cell main+a; the visibility sits at
+       * main + s/G, so the sample distance is a - s/G */
+      double x = (double)(ap - S / 2 + 1) - (double)s / G;
+      g[s * S + ap] = exp(-x * x / (2.0 * sigma * sigma));
+    }
+  if (gcf) oracle_gcf_from_1d(gcf, g, S, G);
+  if (!g1) free(g);
+}

@@ -1,0 +1,79 @@
+/*
+ * CPU oracle for the convolutional gridder -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's CPU gridder and of the integer
+ * steps of its GPU driver.  Only tests, the smoke check and the CPU-baseline
+ * leg of the benchmark may load this library, and only as the checker; the
+ * product path (libgg.so) never links or calls it.
+ *
+ * Reference files cited below are paths within the NVIDIA/SKA-gpu-grid
+ * project (grid.cu, grid_gpu.cu).
+ */
+#ifndef GRID_ORACLE_H
+#define GRID_ORACLE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Restates gridCPU_pz (grid.cu:140-193).
+ *   out_planar : 2*pols*img_dim^2 doubles; real plane [p][y][x] followed by
+ *                the imaginary plane (grid.cu:153-154).  ACCUMULATES (+=),
+ *                exactly like the reference, which never zeroes its output.
+ *   uv         : npts (u,v) pairs in grid-pixel units (CmplxType in[]).
+ *   vals       : npts*pols complex values, interleaved (re,im).
+ *   gcf        : the UN-offset table, gcf_grid^2 * gcf_dim^2 complex values,
+ *                laid out [sub_y*gcf_grid+sub_x][b'][a'] (grid.cu:169-172
+ *                after the centre offset of grid.cu:152).
+ *   debug1     : nonzero = the reference's DEBUG1 footprint mode
+ *                (grid.cu:180-182): adds (1, n) instead of val*gcf.
+ */
+void oracle_grid_pz(double *out_planar, const double *uv, const double *vals,
+                    size_t npts, size_t img_dim, const double *gcf,
+                    size_t gcf_dim, int gcf_grid, int pols, int debug1);
+
+/* Same result, bit for bit: the img_dim rows are split into nthreads bands
+ * and every band walks all visibilities in input order, so each cell sees
+ * the same additions in the same order as oracle_grid_pz. */
+void oracle_grid_pz_mt(double *out_planar, const double *uv,
+                       const double *vals, size_t npts, size_t img_dim,
+                       const double *gcf, size_t gcf_dim, int gcf_grid,
+                       int pols, int debug1, int nthreads);
+
+/* The index step of gridCPU_pz (grid.cu:159-163): main = floor(u),
+ * sub = floorf(G*(u - floorf(u))) with the float conversions C applies.
+ * Writes packed (main*G+sub) pairs like vis2ints (grid_gpu.cu:352-365). */
+void oracle_vis2ints(const double *uv, size_t npts, int gcf_grid,
+                     int32_t *packed_xy);
+
+/* vis2ints as the GPU driver computes it, entirely in double
+ * (grid_gpu.cu:357-363).  Agrees with oracle_vis2ints whenever u and v are
+ * float-representable. */
+void oracle_vis2ints_gpu_formula(const double *uv, size_t npts, int gcf_grid,
+                                 int32_t *packed_xy);
+
+/* Restates set_bookmarks (grid_gpu.cu:366-390) for packed ints sorted by
+ * tile: bookmarks[z] = index of the first visibility whose tile id is >= z,
+ * for z in [0, ntiles]; tile id = (main_y/blocksize)*blockgrid +
+ * main_x/blocksize.  Entries past the last occupied tile are npts. */
+void oracle_set_bookmarks(const int32_t *packed_xy, size_t npts, int gcf_grid,
+                          int blocksize, int blockgrid, int32_t *bookmarks);
+
+/* Separable Gaussian GCF table in the reference's layout (see
+ * oracle_grid_pz): value(sx,sy,a',b') = g(a'-S/2+1 - sx/G) * g(b'-S/2+1 -
+ * sy/G), g(x) = exp(-x^2/(2 sigma^2)), imaginary part 0.  g1 receives the
+ * [G][S] one-dimensional factors (may be NULL). */
+void oracle_gaussian_gcf(double *gcf, double *g1, int gcf_dim, int gcf_grid,
+                         double sigma);
+
+/* Builds the 2-D table from given 1-D factors g1[G][S]: an exact product,
+ * identical on every IEEE-754 host. */
+void oracle_gcf_from_1d(double *gcf, const double *g1, int gcf_dim,
+                        int gcf_grid);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

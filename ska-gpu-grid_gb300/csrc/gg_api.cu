@@ -1,0 +1,976 @@
+// C ABI of the gridder (include/gg.h): contexts, plans, drop-in entry points.
+//
+// The reference's gridGPU (grid_gpu.cu:675-819) pins the caller's buffers,
+// allocates and frees device memory on every call, zeroes the padded grid,
+// launches one compile-time-selected method and copies the whole padded grid
+// back, printing (not returning) any CUDA error.  Here a context owns every
+// device buffer (grown on demand, reused across calls), a plan turns a batch
+// of jobs into device tables once, and executing a plan only enqueues
+// kernels and memsets on the caller's stream, so it can be captured into a
+// CUDA graph.  Errors come back as status codes with a message.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gg_internal.h"
+
+namespace gg {
+
+static thread_local std::string g_last_error;
+static std::atomic<long long> g_launches{0};
+
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+static int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+static int cuda_fail(cudaError_t e, const char *what) {
+  return fail(e == cudaErrorMemoryAllocation ? GG_ERR_NOMEM : GG_ERR_CUDA,
+              "%s: %s", what, cudaGetErrorString(e));
+}
+#define GG_CUDA(call)                                   \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+static bool is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
+static int ilog2(int64_t v) {
+  int l = 0;
+  while ((1ll << l) < v) ++l;
+  return l;
+}
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// ---------------------------------------------------------------------------
+// device buffer that only grows
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void *p = nullptr;
+  size_t n = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= n) return GG_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    size_t want = align256(bytes + bytes / 8);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return cuda_fail(e, "cudaMalloc(workspace)");
+    }
+    n = want;
+    return GG_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+struct HostBuf {
+  void *p = nullptr;
+  size_t n = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= n) return GG_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    size_t want = align256(bytes + bytes / 8 + 4096);
+    cudaError_t e = cudaMallocHost(&p, want);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return cuda_fail(e, "cudaMallocHost(staging)");
+    }
+    n = want;
+    return GG_OK;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace gg
+
+using namespace gg;
+
+// ---------------------------------------------------------------------------
+// options
+// ---------------------------------------------------------------------------
+static gg_options default_opts() {
+  gg_options o;
+  memset(&o, 0, sizeof o);
+  o.mode = GG_MODE_SCATTER;
+  o.layout = GG_LAYOUT_REFERENCE;
+  o.accum = GG_ACC_PLAIN;
+  o.gcf_kind = GG_GCF_TABLE;
+  o.oversample = 8;
+  o.polarizations = 1;
+  o.tile = 32;
+  o.input_sorted = 0;
+  o.gcf_sigma = 0.0;
+  o.window_chunk = 0;
+  return o;
+}
+
+static std::mutex g_opt_mu;
+static gg_options g_global_opts = default_opts();
+
+static int check_options(const gg_options *o) {
+  if (!o) return fail(GG_ERR_ARG, "options: null");
+  if (o->mode < GG_MODE_SCATTER || o->mode > GG_MODE_AUTO)
+    return fail(GG_ERR_ARG, "options: mode %d unknown", o->mode);
+  if (o->layout < GG_LAYOUT_INTERLEAVED || o->layout > GG_LAYOUT_REFERENCE)
+    return fail(GG_ERR_ARG, "options: layout %d unknown", o->layout);
+  if (o->accum != GG_ACC_PLAIN && o->accum != GG_ACC_COMPENSATED)
+    return fail(GG_ERR_ARG, "options: accum %d unknown", o->accum);
+  if (o->gcf_kind < GG_GCF_TABLE || o->gcf_kind > GG_GCF_COUNT)
+    return fail(GG_ERR_ARG, "options: gcf_kind %d unknown", o->gcf_kind);
+  if (!is_pow2(o->oversample) || o->oversample > 64)
+    return fail(GG_ERR_ARG, "options: oversample %d must be a power of two <= 64",
+                o->oversample);
+  if (o->polarizations < 1 || o->polarizations > kMaxPols)
+    return fail(GG_ERR_ARG, "options: polarizations %d outside 1..%d",
+                o->polarizations, kMaxPols);
+  if (!is_pow2(o->tile) || o->tile < 16 || o->tile > 256)
+    return fail(GG_ERR_ARG, "options: tile %d must be a power of two in 16..256",
+                o->tile);
+  if (o->window_chunk < 0) return fail(GG_ERR_ARG, "options: window_chunk < 0");
+  return GG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// context and plan
+// ---------------------------------------------------------------------------
+struct Plan {
+  // resolved launch configuration
+  int mode = GG_MODE_WINDOW;
+  int accum = GG_ACC_PLAIN;
+  int vals_f64 = 0;
+  int gauss = 0;
+  float sigma = 0.f;
+  int G = 8, P = 1, T = 32, chunk = 2048;
+  int njobs = 0;
+  int64_t total_vis = 0;
+  int total_tiles = 0;
+  int input_sorted = 0;
+  int comp_lo = 0;  // compensated scatter with complex64 output
+  struct ClassRange {
+    int S, j0, j1;
+    int64_t v0, v1;  // global vis range
+    int t0, t1;      // global tile range
+  };
+  std::vector<ClassRange> classes;
+  std::vector<JobDesc> hjobs;
+  std::vector<BinJob> hbin;
+  std::vector<int64_t> hvis_base;
+  std::vector<int> htile_base, hclass;
+  std::vector<std::pair<void *, size_t>> zero_ranges;  // outputs to clear
+  std::vector<std::pair<float *, int64_t>> finalize;   // (out, floats) comp scatter
+  std::vector<std::pair<void *, int64_t>> count_fill;  // (vals, npts) DEBUG1
+  // workspace carve (offsets into the device workspace)
+  size_t o_jobs, o_bin, o_visb, o_tileb, o_class, o_packed, o_key, o_bm,
+      o_cursor, o_scan, o_sidx, o_svals, o_order, o_items, o_kept, o_lo,
+      o_count_vals, o_count_gcf, ws_bytes;
+  int64_t vstride = 0, class_cap = 0;
+  size_t table_bytes = 0;  // bytes uploaded from staging (jobs..class)
+};
+
+struct gg_context {
+  int device = 0;
+  int sm_count = 152;
+  std::mutex mu;
+  DevBuf ws;        // plan workspace
+  DevBuf flags;     // int32[16]: flags[0..7], item counters [8..11], item_next [12..15]
+  HostBuf staging;  // pinned: device tables are uploaded from here
+  cudaEvent_t upload_done = nullptr;  // staging may be rewritten after this
+  cudaEvent_t exec_done = nullptr;    // workspace free after this
+  cudaStream_t own = nullptr;         // stream of the host-path calls
+  // host-path device copies of the caller's buffers
+  DevBuf h_uv, h_vals, h_gcf, h_out;
+  Plan plan;
+  // profiling: events around set-up+binning, gridding kernels, whole call
+  int profile = 0;
+  int prof_recorded = 0;
+  cudaEvent_t prof[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+static int ctx_init(gg_context *c, int device) {
+  c->device = device;
+  GG_CUDA(cudaSetDevice(device));
+  int sms = 0;
+  GG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  c->sm_count = sms;
+  GG_CUDA(cudaEventCreateWithFlags(&c->upload_done, cudaEventDisableTiming));
+  GG_CUDA(cudaEventCreateWithFlags(&c->exec_done, cudaEventDisableTiming));
+  GG_CUDA(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking));
+  for (auto &e : c->prof) GG_CUDA(cudaEventCreate(&e));
+  int st = c->flags.ensure(64 * sizeof(int));
+  if (st) return st;
+  GG_CUDA(cudaMemset(c->flags.p, 0, 64 * sizeof(int)));
+  return GG_OK;
+}
+
+static void ctx_release(gg_context *c) {
+  cudaSetDevice(c->device);
+  if (c->exec_done) cudaEventSynchronize(c->exec_done);
+  c->ws.release();
+  c->flags.release();
+  c->h_uv.release();
+  c->h_vals.release();
+  c->h_gcf.release();
+  c->h_out.release();
+  c->staging.release();
+  if (c->upload_done) cudaEventDestroy(c->upload_done);
+  if (c->exec_done) cudaEventDestroy(c->exec_done);
+  for (auto &e : c->prof)
+    if (e) cudaEventDestroy(e);
+  if (c->own) cudaStreamDestroy(c->own);
+}
+
+static int resolve_mode(const gg_options *o, int S) {
+  if (o->mode != GG_MODE_AUTO) return o->mode;
+  (void)S;
+  return GG_MODE_WINDOW;  // measured fastest at every size class so far
+}
+
+// Build the plan for a batch: validate, resolve, order jobs by support class,
+// lay out the workspace.  No device work.
+static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
+                      int njobs, Plan &pl) {
+  int st = check_options(opt);
+  if (st) return st;
+  if (njobs < 1) return fail(GG_ERR_ARG, "no jobs");
+  if (!jobs) return fail(GG_ERR_ARG, "jobs: null");
+  pl = Plan();
+  pl.G = opt->oversample;
+  pl.P = opt->polarizations;
+  pl.T = opt->tile;
+  pl.chunk = opt->window_chunk > 0 ? opt->window_chunk : 2048;
+  pl.input_sorted = opt->input_sorted ? 1 : 0;
+  pl.gauss = opt->gcf_kind == GG_GCF_GAUSSIAN;
+  pl.accum = opt->accum;
+  pl.njobs = njobs;
+  const int vt = jobs[0].vals_type;
+  if (vt != GG_C64 && vt != GG_C128) return fail(GG_ERR_ARG, "job 0: vals_type %d", vt);
+  pl.vals_f64 = vt == GG_C128;
+  const size_t vbytes = pl.vals_f64 ? 16 : 8;
+  int mode = -1;
+  double sigma = -1.0;
+  // stable order by support
+  std::vector<int> order(njobs);
+  for (int j = 0; j < njobs; ++j) order[j] = j;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return jobs[a].gcf_dim < jobs[b].gcf_dim;
+  });
+  int64_t vis = 0;
+  int64_t tiles = 0;
+  for (int k = 0; k < njobs; ++k) {
+    const gg_job &J = jobs[order[k]];
+    const int j = order[k];
+    if (J.vals_type != vt)
+      return fail(GG_ERR_ARG, "job %d: all jobs of a batch need the same vals_type", j);
+    if (J.uv_type != GG_C64 && J.uv_type != GG_C128)
+      return fail(GG_ERR_ARG, "job %d: uv_type %d", j, J.uv_type);
+    if (J.out_type != GG_C64 && J.out_type != GG_C128)
+      return fail(GG_ERR_ARG, "job %d: out_type %d", j, J.out_type);
+    if (pl.vals_f64 && J.out_type != GG_C128)
+      return fail(GG_ERR_ARG,
+                  "job %d: complex128 values need a complex128 grid (the reference "
+                  "instantiates gridGPU<double2,double2> only)", j);
+    if (J.gcf_dim != 4 && J.gcf_dim != 8 && J.gcf_dim != 16 && J.gcf_dim != 32)
+      return fail(GG_ERR_ARG, "job %d: gcf_dim %lld not in {4,8,16,32}", j,
+                  (long long)J.gcf_dim);
+    if (J.img_dim < 1 || J.img_dim > 32768)
+      return fail(GG_ERR_ARG, "job %d: img_dim %lld outside 1..32768", j,
+                  (long long)J.img_dim);
+    if (J.npts < 0) return fail(GG_ERR_ARG, "job %d: npts < 0", j);
+    if (!J.out) return fail(GG_ERR_ARG, "job %d: out is null", j);
+    if (J.npts > 0 && (!J.uv || !J.vals))
+      return fail(GG_ERR_ARG, "job %d: uv/vals null", j);
+    if (opt->gcf_kind == GG_GCF_TABLE && !J.gcf)
+      return fail(GG_ERR_ARG, "job %d: TABLE GCF needs gcf", j);
+    const int m = resolve_mode(opt, (int)J.gcf_dim);
+    if (mode < 0) mode = m;
+    if (m != mode) return fail(GG_ERR_ARG, "job %d: mixed methods in one batch", j);
+    double sg = J.gcf_sigma > 0 ? J.gcf_sigma
+                                : (opt->gcf_sigma > 0 ? opt->gcf_sigma : J.gcf_dim / 4.0);
+    if (pl.gauss) {
+      if (sigma < 0) sigma = sg;
+      if (sg != sigma)
+        return fail(GG_ERR_ARG, "job %d: on-the-fly GCF needs one sigma per batch", j);
+      if (J.gcf_dim != jobs[order[0]].gcf_dim)
+        return fail(GG_ERR_ARG, "on-the-fly GCF needs one support per batch");
+    }
+    if (mode == GG_MODE_GATHER && pl.T != 32)
+      return fail(GG_ERR_ARG, "gather needs tile 32");
+    vis += J.npts;
+    int ntx = (int)((J.img_dim + pl.T - 1) / pl.T);
+    tiles += (int64_t)ntx * ntx;
+  }
+  if (vis >= (1ll << 31) - 1024) return fail(GG_ERR_ARG, "batch has >= 2^31 visibilities");
+  if (tiles >= (1ll << 30)) return fail(GG_ERR_ARG, "batch has too many uv tiles");
+  pl.mode = mode;
+  pl.sigma = (float)(sigma > 0 ? sigma : 0.0);
+  pl.total_vis = vis;
+  pl.total_tiles = (int)tiles;
+  if (pl.vals_f64) pl.accum = GG_ACC_PLAIN;  // FP64 values: FP64 arithmetic
+  const bool binned = mode != GG_MODE_SCATTER;
+
+  // workspace layout
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off = align256(off + bytes);
+    return o;
+  };
+  pl.o_jobs = take(sizeof(JobDesc) * njobs);
+  pl.o_bin = take(sizeof(BinJob) * njobs);
+  pl.o_visb = take(sizeof(int64_t) * (njobs + 1));
+  pl.o_tileb = take(sizeof(int) * (njobs + 1));
+  pl.o_class = take(sizeof(int) * njobs);
+  pl.table_bytes = off;
+  pl.vstride = vis + 8;
+  pl.class_cap = tiles + vis / pl.chunk + njobs + 1;
+  if (binned) {
+    pl.o_packed = take(sizeof(int2) * (vis + 1));
+    pl.o_key = take(sizeof(int) * (vis + 1));
+    pl.o_bm = take(sizeof(int) * (tiles + 8));
+    pl.o_cursor = take(sizeof(int) * (tiles + 8));
+    pl.o_scan = take(sizeof(int) * scan_tmp_ints(std::max<int64_t>(tiles + 1, vis + 1)));
+    pl.o_sidx = take(sizeof(int2) * (vis + 8));
+    pl.o_svals = take(vbytes * pl.P * pl.vstride + 64);
+    pl.o_order = 0;
+    pl.o_kept = pl.input_sorted ? take(sizeof(int) * (vis + 8)) : 0;
+    pl.o_items = mode == GG_MODE_WINDOW ? take(sizeof(WorkItem) * 4 * pl.class_cap) : 0;
+  }
+  const bool count = opt->gcf_kind == GG_GCF_COUNT;
+  pl.o_count_vals = count ? take(vbytes * pl.P * (vis + 1)) : 0;
+  int maxS = 0;
+  for (int j = 0; j < njobs; ++j) maxS = std::max<int>(maxS, (int)jobs[j].gcf_dim);
+  pl.o_count_gcf = count ? take(vbytes * pl.G * pl.G * maxS * maxS) : 0;
+  pl.comp_lo = mode == GG_MODE_SCATTER && pl.accum == GG_ACC_COMPENSATED && !pl.vals_f64;
+  size_t lo_total = 0;
+  if (pl.comp_lo)
+    for (int j = 0; j < njobs; ++j)
+      if (jobs[j].out_type == GG_C64)
+        lo_total += align256(8 * (size_t)pl.P * jobs[j].img_dim * jobs[j].img_dim);
+  pl.o_lo = pl.comp_lo ? take(lo_total) : 0;
+  pl.ws_bytes = off;
+
+  // host tables in class order
+  pl.hjobs.resize(njobs);
+  pl.hbin.resize(njobs);
+  pl.hvis_base.resize(njobs + 1);
+  pl.htile_base.resize(njobs + 1);
+  pl.hclass.resize(njobs);
+  int64_t vb = 0;
+  int tb = 0;
+  size_t lo_off = 0;
+  int64_t cnt_off = 0;
+  for (int k = 0; k < njobs; ++k) {
+    const gg_job &J = jobs[order[k]];
+    const int S = (int)J.gcf_dim;
+    if (pl.classes.empty() || pl.classes.back().S != S) {
+      if (!pl.classes.empty()) {
+        pl.classes.back().j1 = k;
+        pl.classes.back().v1 = vb;
+        pl.classes.back().t1 = tb;
+      }
+      pl.classes.push_back({S, k, k, vb, vb, tb, tb});
+    }
+    const int N = (int)J.img_dim;
+    const int ntx = (N + pl.T - 1) / pl.T;
+    JobDesc &D = pl.hjobs[k];
+    memset(&D, 0, sizeof D);
+    D.out = J.out;
+    D.uv = J.uv;
+    D.vals = J.vals;
+    D.gcf = J.gcf;
+    D.npts = J.npts;
+    D.vstride = pl.vstride;
+    D.N = N;
+    D.S = S;
+    D.G = pl.G;
+    D.log2G = ilog2(pl.G);
+    D.P = pl.P;
+    D.T = pl.T;
+    D.log2T = ilog2(pl.T);
+    D.ntx = ntx;
+    int layout = opt->layout;
+    if (layout == GG_LAYOUT_REFERENCE)
+      layout = mode == GG_MODE_WINDOW ? GG_LAYOUT_PLANAR : GG_LAYOUT_INTERLEAVED;
+    D.planar = layout == GG_LAYOUT_PLANAR;
+    D.out_f64 = J.out_type == GG_C128;
+    D.uv_f64 = J.uv_type == GG_C128;
+    D.sigma = pl.sigma;
+    BinJob &B = pl.hbin[k];
+    memset(&B, 0, sizeof B);
+    B.uv = J.uv;
+    B.vals = J.vals;
+    B.vis_base = vb;
+    B.npts = J.npts;
+    B.tile_base = tb;
+    B.ntiles = ntx * ntx;
+    B.N = N;
+    B.S = S;
+    B.G = pl.G;
+    B.log2G = D.log2G;
+    B.log2T = D.log2T;
+    B.ntx = ntx;
+    B.P = pl.P;
+    B.uv_f64 = D.uv_f64;
+    pl.hvis_base[k] = vb;
+    pl.htile_base[k] = tb;
+    pl.hclass[k] = (int)pl.classes.size() - 1;
+    const size_t out_bytes = (size_t)(D.out_f64 ? 16 : 8) * pl.P * N * N;
+    if (mode != GG_MODE_GATHER) pl.zero_ranges.push_back({J.out, out_bytes});
+    if (pl.comp_lo && J.out_type == GG_C64) {
+      // filled in once the workspace base is known (plan_bind)
+      D.lo = reinterpret_cast<float *>(lo_off + 1);
+      pl.finalize.push_back({(float *)J.out, (int64_t)2 * pl.P * N * N});
+      lo_off += align256(out_bytes);
+    }
+    if (count) {
+      pl.count_fill.push_back({reinterpret_cast<void *>(cnt_off), J.npts});
+      cnt_off += J.npts * pl.P;
+    }
+    vb += J.npts;
+    tb += ntx * ntx;
+  }
+  pl.classes.back().j1 = njobs;
+  pl.classes.back().v1 = vb;
+  pl.classes.back().t1 = tb;
+  pl.hvis_base[njobs] = vb;
+  pl.htile_base[njobs] = tb;
+  return GG_OK;
+}
+
+// Fix device addresses once the workspace exists; write tables to staging.
+static int plan_bind(gg_context *c, const gg_options *opt, Plan &pl) {
+  int st = c->ws.ensure(pl.ws_bytes);
+  if (st) return st;
+  char *ws = (char *)c->ws.p;
+  const bool binned = pl.mode != GG_MODE_SCATTER;
+  const size_t vbytes = pl.vals_f64 ? 16 : 8;
+  for (int k = 0; k < pl.njobs; ++k) {
+    JobDesc &D = pl.hjobs[k];
+    if (pl.comp_lo && D.lo) D.lo = (float *)(ws + pl.o_lo + ((size_t)D.lo - 1));
+    if (opt->gcf_kind == GG_GCF_COUNT) {
+      void *cv = ws + pl.o_count_vals +
+                 vbytes * (size_t)reinterpret_cast<intptr_t>(pl.count_fill[k].first);
+      D.vals = cv;
+      pl.hbin[k].vals = cv;
+      D.gcf = ws + pl.o_count_gcf;
+    }
+    if (binned) {
+      D.idx = (const int2 *)(ws + pl.o_sidx);
+      D.vals = ws + pl.o_svals;
+      D.bookmarks = (const int *)(ws + pl.o_bm) + pl.htile_base[k];
+    }
+  }
+  // count-mode fills: resolve to absolute addresses
+  for (auto &f : pl.count_fill)
+    f.first = ws + pl.o_count_vals + vbytes * (size_t)reinterpret_cast<intptr_t>(f.first);
+  // pinned staging: wait until the previous upload has been consumed
+  GG_CUDA(cudaEventSynchronize(c->upload_done));
+  st = c->staging.ensure(pl.table_bytes);
+  if (st) return st;
+  char *h = (char *)c->staging.p;
+  memcpy(h + pl.o_jobs, pl.hjobs.data(), sizeof(JobDesc) * pl.njobs);
+  memcpy(h + pl.o_bin, pl.hbin.data(), sizeof(BinJob) * pl.njobs);
+  memcpy(h + pl.o_visb, pl.hvis_base.data(), sizeof(int64_t) * (pl.njobs + 1));
+  memcpy(h + pl.o_tileb, pl.htile_base.data(), sizeof(int) * (pl.njobs + 1));
+  memcpy(h + pl.o_class, pl.hclass.data(), sizeof(int) * pl.njobs);
+  return GG_OK;
+}
+
+// Enqueue the whole computation on stream s.
+static int plan_execute(gg_context *c, const gg_options *opt, Plan &pl,
+                        cudaStream_t s) {
+  char *ws = (char *)c->ws.p;
+  int *flags = (int *)c->flags.p;
+  GG_CUDA(cudaStreamWaitEvent(s, c->exec_done, 0));
+  if (c->profile) GG_CUDA(cudaEventRecord(c->prof[0], s));
+  GG_CUDA(cudaMemcpyAsync(ws, c->staging.p, pl.table_bytes, cudaMemcpyHostToDevice, s));
+  GG_CUDA(cudaEventRecord(c->upload_done, s));
+  const JobDesc *djobs = (const JobDesc *)(ws + pl.o_jobs);
+  const int64_t *dvisb = (const int64_t *)(ws + pl.o_visb);
+  const int *dtileb = (const int *)(ws + pl.o_tileb);
+  const int *dclass = (const int *)(ws + pl.o_class);
+  const size_t vbytes = pl.vals_f64 ? 16 : 8;
+
+  for (auto &z : pl.zero_ranges) GG_CUDA(cudaMemsetAsync(z.first, 0, z.second, s));
+  if (pl.comp_lo) {
+    size_t lo_bytes = pl.ws_bytes - pl.o_lo;
+    GG_CUDA(cudaMemsetAsync(ws + pl.o_lo, 0, lo_bytes, s));
+  }
+  if (opt->gcf_kind == GG_GCF_COUNT) {
+    int maxS = 0;
+    for (auto &cl : pl.classes) maxS = std::max(maxS, cl.S);
+    for (size_t k = 0; k < pl.count_fill.size(); ++k) {
+      GG_CUDA(launch_count_inputs(pl.count_fill[k].first, pl.vals_f64,
+                                  pl.count_fill[k].second, pl.P,
+                                  k == 0 ? (void *)(ws + pl.o_count_gcf) : nullptr,
+                                  k == 0 ? (int64_t)pl.G * pl.G * maxS * maxS : 0, s));
+    }
+  }
+
+  GridLaunch g{};
+  g.accum = pl.accum;
+  g.vals_f64 = pl.vals_f64;
+  g.gauss = pl.gauss;
+  g.sigma = pl.sigma;
+  g.G = pl.G;
+  g.tile = pl.T;
+  g.P = pl.P;
+  g.flags = flags;
+  g.sm_count = c->sm_count;
+
+  if (pl.mode != GG_MODE_SCATTER) {
+    BinBuffers b{};
+    b.jobs = (const BinJob *)(ws + pl.o_bin);
+    b.vis_base = dvisb;
+    b.tile_base = dtileb;
+    b.njobs = pl.njobs;
+    b.total_vis = pl.total_vis;
+    b.total_tiles = pl.total_tiles;
+    b.vals_bytes = (int)vbytes;
+    b.P = pl.P;
+    b.packed = (int2 *)(ws + pl.o_packed);
+    b.key = (int *)(ws + pl.o_key);
+    b.bookmarks = (int *)(ws + pl.o_bm);
+    b.cursor = (int *)(ws + pl.o_cursor);
+    b.scan_tmp = (int *)(ws + pl.o_scan);
+    b.sorted_idx = (int2 *)(ws + pl.o_sidx);
+    b.sorted_vals = ws + pl.o_svals;
+    b.vstride = pl.vstride;
+    b.order = nullptr;
+    b.flags = flags;
+    b.input_sorted = pl.input_sorted;
+    b.kept_pos = pl.input_sorted ? (int *)(ws + pl.o_kept) : nullptr;
+    GG_CUDA(run_binning(b, s));
+  }
+
+  if (pl.mode == GG_MODE_WINDOW) {
+    GG_CUDA(cudaMemsetAsync(flags + 8, 0, 8 * sizeof(int), s));
+    WorkItem *items = (WorkItem *)(ws + pl.o_items);
+    GG_CUDA(launch_make_items((const int *)(ws + pl.o_bm), dtileb, dclass, pl.njobs,
+                              pl.total_tiles, pl.chunk, items, pl.class_cap, flags + 8, s));
+    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[1], s));
+    for (size_t ci = 0; ci < pl.classes.size(); ++ci) {
+      const auto &cl = pl.classes[ci];
+      g.jobs = djobs;
+      g.njobs = pl.njobs;
+      g.S = cl.S;
+      g.items = items + ci * pl.class_cap;
+      g.nitems = flags + 8 + ci;
+      g.item_next = flags + 12 + ci;
+      g.max_items = pl.class_cap;
+      GG_CUDA(launch_window(g, s));
+    }
+    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[2], s));
+  } else if (pl.mode == GG_MODE_GATHER) {
+    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[1], s));
+    for (const auto &cl : pl.classes) {
+      g.jobs = djobs + cl.j0;
+      g.njobs = cl.j1 - cl.j0;
+      g.S = cl.S;
+      g.tile_base = dtileb + cl.j0;
+      g.total_tiles = cl.t1 - cl.t0;
+      GG_CUDA(launch_gather(g, s));
+    }
+    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[2], s));
+  } else {
+    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[1], s));
+    for (const auto &cl : pl.classes) {
+      g.jobs = djobs + cl.j0;
+      g.njobs = cl.j1 - cl.j0;
+      g.S = cl.S;
+      g.vis_base = dvisb + cl.j0;
+      g.total_vis = cl.v1 - cl.v0;
+      GG_CUDA(launch_scatter(g, s));
+    }
+    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[2], s));
+    if (pl.comp_lo) {
+      for (int k = 0; k < pl.njobs; ++k) {
+        const JobDesc &D = pl.hjobs[k];
+        if (D.lo)
+          GG_CUDA(launch_comp_finalize((float *)D.out, D.lo, 2ll * pl.P * D.N * D.N, s));
+      }
+    }
+  }
+  if (c->profile) {
+    GG_CUDA(cudaEventRecord(c->prof[3], s));
+    c->prof_recorded = 1;
+  }
+  GG_CUDA(cudaEventRecord(c->exec_done, s));
+  return GG_OK;
+}
+
+static int grid_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs,
+                     int njobs, cudaStream_t s) {
+  GG_CUDA(cudaSetDevice(c->device));
+  Plan &pl = c->plan;
+  int st = plan_build(c, opt, jobs, njobs, pl);
+  if (st) return st;
+  // the workspace may be reallocated: earlier work on it must be finished
+  if (pl.ws_bytes > c->ws.n) GG_CUDA(cudaEventSynchronize(c->exec_done));
+  st = plan_bind(c, opt, pl);
+  if (st) return st;
+  return plan_execute(c, opt, pl, s);
+}
+
+// ---------------------------------------------------------------------------
+// exported ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int gg_abi_version(void) { return GG_ABI_VERSION; }
+const char *gg_last_error(void) { return g_last_error.c_str(); }
+
+int gg_default_options(gg_options *opt) {
+  if (!opt) return fail(GG_ERR_ARG, "opt: null");
+  *opt = default_opts();
+  return GG_OK;
+}
+int gg_set_global_options(const gg_options *opt) {
+  int st = check_options(opt);
+  if (st) return st;
+  std::lock_guard<std::mutex> lk(g_opt_mu);
+  g_global_opts = *opt;
+  return GG_OK;
+}
+int gg_get_global_options(gg_options *opt) {
+  if (!opt) return fail(GG_ERR_ARG, "opt: null");
+  std::lock_guard<std::mutex> lk(g_opt_mu);
+  *opt = g_global_opts;
+  return GG_OK;
+}
+
+int gg_create(gg_context **ctx, int device) {
+  if (!ctx) return fail(GG_ERR_ARG, "ctx: null");
+  *ctx = nullptr;
+  std::unique_ptr<gg_context> c(new (std::nothrow) gg_context);
+  if (!c) return fail(GG_ERR_NOMEM, "context allocation");
+  int st = ctx_init(c.get(), device);
+  if (st) {
+    ctx_release(c.get());
+    return st;
+  }
+  *ctx = c.release();
+  return GG_OK;
+}
+
+int gg_destroy(gg_context *ctx) {
+  if (!ctx) return GG_OK;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx_release(ctx);
+  }
+  delete ctx;
+  return GG_OK;
+}
+
+int gg_reserve(gg_context *ctx, const gg_options *opt, int64_t max_npts,
+               int64_t max_img_dim, int64_t max_gcf_dim, int32_t vals_type) {
+  if (!ctx) return fail(GG_ERR_ARG, "ctx: null");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  GG_CUDA(cudaSetDevice(ctx->device));
+  gg_job j;
+  memset(&j, 0, sizeof j);
+  j.out = (void *)16;
+  j.uv = (const void *)16;
+  j.vals = (const void *)16;
+  j.gcf = (const void *)16;
+  j.npts = max_npts;
+  j.img_dim = max_img_dim;
+  j.gcf_dim = max_gcf_dim;
+  j.uv_type = GG_C128;
+  j.vals_type = vals_type;
+  j.out_type = GG_C128;
+  Plan pl;
+  int st = plan_build(ctx, opt, &j, 1, pl);
+  if (st) return st;
+  GG_CUDA(cudaEventSynchronize(ctx->exec_done));
+  st = ctx->ws.ensure(pl.ws_bytes);
+  if (st) return st;
+  return ctx->staging.ensure(pl.table_bytes + 4096);
+}
+
+int gg_workspace_bytes(gg_context *ctx, size_t *bytes) {
+  if (!ctx || !bytes) return fail(GG_ERR_ARG, "null argument");
+  *bytes = ctx->ws.n;
+  return GG_OK;
+}
+
+int gg_grid_device(gg_context *ctx, const gg_options *opt, const gg_job *job,
+                   void *stream) {
+  if (!ctx) return fail(GG_ERR_ARG, "ctx: null");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  return grid_jobs(ctx, opt, job, 1, (cudaStream_t)stream);
+}
+
+int gg_grid_batch(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
+                  int32_t njobs, void *stream) {
+  if (!ctx) return fail(GG_ERR_ARG, "ctx: null");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  return grid_jobs(ctx, opt, jobs, njobs, (cudaStream_t)stream);
+}
+
+int gg_read_flags(gg_context *ctx, void *stream, int32_t flags[4]) {
+  if (!ctx || !flags) return fail(GG_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  GG_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  int h[4];
+  GG_CUDA(cudaMemcpyAsync(h, ctx->flags.p, sizeof h, cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  GG_CUDA(cudaMemsetAsync(ctx->flags.p, 0, sizeof h, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < 4; ++i) flags[i] = h[i];
+  return GG_OK;
+}
+
+int gg_profile_enable(gg_context *ctx, int on) {
+  if (!ctx) return fail(GG_ERR_ARG, "ctx: null");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->profile = on ? 1 : 0;
+  ctx->prof_recorded = 0;
+  return GG_OK;
+}
+
+int gg_profile_last(gg_context *ctx, double ms[3]) {
+  if (!ctx || !ms) return fail(GG_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!ctx->profile || !ctx->prof_recorded)
+    return fail(GG_ERR_STATE, "profiling off or no call recorded");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  GG_CUDA(cudaEventSynchronize(ctx->prof[3]));
+  float a = 0, b = 0, t = 0;
+  GG_CUDA(cudaEventElapsedTime(&a, ctx->prof[0], ctx->prof[1]));
+  GG_CUDA(cudaEventElapsedTime(&b, ctx->prof[1], ctx->prof[2]));
+  GG_CUDA(cudaEventElapsedTime(&t, ctx->prof[0], ctx->prof[3]));
+  ms[0] = a;
+  ms[1] = b;
+  ms[2] = t;
+  return GG_OK;
+}
+
+int gg_kernel_launches(int64_t *count) {
+  if (!count) return fail(GG_ERR_ARG, "count: null");
+  *count = (int64_t)g_launches.load();
+  return GG_OK;
+}
+
+int gg_vis2ints(int uv_type, const void *uv, int64_t npts, int32_t oversample,
+                int32_t *packed, void *stream) {
+  if (npts < 0 || (npts > 0 && (!uv || !packed)))
+    return fail(GG_ERR_ARG, "vis2ints: bad arguments");
+  if (uv_type != GG_C64 && uv_type != GG_C128) return fail(GG_ERR_ARG, "uv_type");
+  if (!is_pow2(oversample) || oversample > 64) return fail(GG_ERR_ARG, "oversample");
+  static int *dflags = nullptr;
+  static std::mutex mu;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!dflags) {
+      GG_CUDA(cudaMalloc(&dflags, 16 * sizeof(int)));
+      GG_CUDA(cudaMemset(dflags, 0, 16 * sizeof(int)));
+    }
+  }
+  GG_CUDA(launch_vis2ints(uv_type == GG_C128, uv, npts, oversample, (int2 *)packed,
+                          dflags, (cudaStream_t)stream));
+  return GG_OK;
+}
+
+int gg_bin(gg_context *ctx, const gg_options *opt, int uv_type, const void *uv,
+           int64_t npts, int64_t img_dim, int64_t gcf_dim, int32_t *bookmarks,
+           int32_t *order, void *stream) {
+  if (!ctx || !bookmarks) return fail(GG_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  GG_CUDA(cudaSetDevice(ctx->device));
+  gg_options o = *opt;
+  o.mode = GG_MODE_GATHER;
+  o.gcf_kind = GG_GCF_GAUSSIAN;  // no table needed; nothing is gridded
+  o.tile = opt->tile;
+  gg_job j;
+  memset(&j, 0, sizeof j);
+  j.out = (void *)16;
+  j.uv = uv;
+  j.vals = uv;  // values are copied along but unused: reuse the uv array
+  j.npts = npts;
+  j.img_dim = img_dim;
+  j.gcf_dim = gcf_dim;
+  j.uv_type = uv_type;
+  j.vals_type = GG_C64;
+  j.out_type = GG_C64;
+  if (o.tile != 32) o.mode = GG_MODE_WINDOW;
+  Plan pl;
+  int st = plan_build(ctx, &o, &j, 1, pl);
+  if (st) return st;
+  pl.P = 1;
+  if (pl.ws_bytes > ctx->ws.n) GG_CUDA(cudaEventSynchronize(ctx->exec_done));
+  size_t order_off = align256(pl.ws_bytes);
+  pl.ws_bytes = order_off + align256(sizeof(int) * (npts + 8));
+  st = plan_bind(ctx, &o, pl);
+  if (st) return st;
+  char *ws = (char *)ctx->ws.p;
+  cudaStream_t s = (cudaStream_t)stream;
+  GG_CUDA(cudaStreamWaitEvent(s, ctx->exec_done, 0));
+  GG_CUDA(cudaMemcpyAsync(ws, ctx->staging.p, pl.table_bytes, cudaMemcpyHostToDevice, s));
+  GG_CUDA(cudaEventRecord(ctx->upload_done, s));
+  BinBuffers b{};
+  b.jobs = (const BinJob *)(ws + pl.o_bin);
+  b.vis_base = (const int64_t *)(ws + pl.o_visb);
+  b.tile_base = (const int *)(ws + pl.o_tileb);
+  b.njobs = 1;
+  b.total_vis = pl.total_vis;
+  b.total_tiles = pl.total_tiles;
+  b.vals_bytes = 8;
+  b.P = 1;
+  b.packed = (int2 *)(ws + pl.o_packed);
+  b.key = (int *)(ws + pl.o_key);
+  b.bookmarks = (int *)(ws + pl.o_bm);
+  b.cursor = (int *)(ws + pl.o_cursor);
+  b.scan_tmp = (int *)(ws + pl.o_scan);
+  b.sorted_idx = (int2 *)(ws + pl.o_sidx);
+  b.sorted_vals = ws + pl.o_svals;
+  b.vstride = pl.vstride;
+  b.order = (int *)(ws + order_off);
+  b.flags = (int *)ctx->flags.p;
+  b.input_sorted = pl.input_sorted;
+  b.kept_pos = pl.input_sorted ? (int *)(ws + pl.o_kept) : nullptr;
+  GG_CUDA(run_binning(b, s));
+  GG_CUDA(cudaMemcpyAsync(bookmarks, b.bookmarks, sizeof(int) * (pl.total_tiles + 1),
+                          cudaMemcpyDeviceToDevice, s));
+  if (order)
+    GG_CUDA(cudaMemcpyAsync(order, b.order, sizeof(int) * npts, cudaMemcpyDeviceToDevice, s));
+  GG_CUDA(cudaEventRecord(ctx->exec_done, s));
+  return GG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// host-buffer entry points (drop-in gridGPU)
+// ---------------------------------------------------------------------------
+static std::mutex g_host_mu;
+static gg_context *g_host_ctx[64];
+
+static int host_ctx(gg_context **out) {
+  int dev = 0;
+  GG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(GG_ERR_ARG, "device %d", dev);
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  if (!g_host_ctx[dev]) {
+    int st = gg_create(&g_host_ctx[dev], dev);
+    if (st) return st;
+  }
+  *out = g_host_ctx[dev];
+  return GG_OK;
+}
+
+extern "C" int gg_grid_host(const gg_options *opt, int out_type, void *out,
+                            int uv_type, const void *uv, int vals_type,
+                            const void *vals, size_t npts, size_t img_dim,
+                            const void *gcf, size_t gcf_dim) {
+  int st = check_options(opt);
+  if (st) return st;
+  if (!out) return fail(GG_ERR_ARG, "out: null");
+  if (npts > 0 && (!uv || !vals)) return fail(GG_ERR_ARG, "in/in_vals: null");
+  if (opt->gcf_kind == GG_GCF_TABLE && !gcf) return fail(GG_ERR_ARG, "gcf: null");
+  gg_context *c = nullptr;
+  if ((st = host_ctx(&c))) return st;
+  std::lock_guard<std::mutex> lk(c->mu);
+  GG_CUDA(cudaSetDevice(c->device));
+  const size_t P = (size_t)opt->polarizations, G = (size_t)opt->oversample;
+  const size_t N = img_dim, S = gcf_dim;
+  const size_t uvb = uv_type == GG_C128 ? 16 : 8, vb = vals_type == GG_C128 ? 16 : 8;
+  const size_t ob = out_type == GG_C128 ? 16 : 8;
+  const size_t grid_elems = P * N * N;
+  const size_t head = N * S + S;
+  const size_t total = (N * N + 2 * N * S + 2 * S) * P;
+  // wait for the previous host call to finish with the device copies
+  GG_CUDA(cudaEventSynchronize(c->exec_done));
+  if ((st = c->h_uv.ensure(uvb * (npts + 1)))) return st;
+  if ((st = c->h_vals.ensure(vb * P * (npts + 1)))) return st;
+  if ((st = c->h_gcf.ensure(vb * G * G * S * S + 16))) return st;
+  if ((st = c->h_out.ensure(ob * grid_elems))) return st;
+  cudaStream_t s = c->own;
+  if (npts) {
+    GG_CUDA(cudaMemcpyAsync(c->h_uv.p, uv, uvb * npts, cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(c->h_vals.p, vals, vb * P * npts, cudaMemcpyHostToDevice, s));
+  }
+  if (opt->gcf_kind == GG_GCF_TABLE)
+    GG_CUDA(cudaMemcpyAsync(c->h_gcf.p, gcf, vb * G * G * S * S, cudaMemcpyHostToDevice, s));
+  gg_job j;
+  memset(&j, 0, sizeof j);
+  j.out = c->h_out.p;
+  j.uv = c->h_uv.p;
+  j.vals = c->h_vals.p;
+  j.gcf = c->h_gcf.p;
+  j.npts = (int64_t)npts;
+  j.img_dim = (int64_t)N;
+  j.gcf_dim = (int64_t)S;
+  j.uv_type = uv_type;
+  j.vals_type = vals_type;
+  j.out_type = out_type;
+  st = grid_jobs(c, opt, &j, 1, s);
+  if (st) return st;
+  char *o = (char *)out;
+  GG_CUDA(cudaMemcpyAsync(o + ob * head, c->h_out.p, ob * grid_elems, cudaMemcpyDeviceToHost, s));
+  memset(o, 0, ob * head);
+  memset(o + ob * (head + grid_elems), 0, ob * (total - head - grid_elems));
+  GG_CUDA(cudaStreamSynchronize(s));
+  int h[4];
+  GG_CUDA(cudaMemcpy(h, c->flags.p, sizeof h, cudaMemcpyDeviceToHost));
+  GG_CUDA(cudaMemset(c->flags.p, 0, sizeof h));
+  if (h[FLAG_TIMEOUT]) return fail(GG_ERR_TIMEOUT, "a bounded device wait expired");
+  if (h[FLAG_UNSORTED])
+    return fail(GG_ERR_UNSORTED, "input_sorted set but visibilities are not tile-sorted");
+  if (h[FLAG_BOUNDS]) return fail(GG_ERR_STATE, "internal: sub-grid bounds check failed");
+  return GG_OK;
+}
+
+static int host_typed(int out_type, void *out, int in_type, const void *in,
+                      const void *vals, size_t npts, size_t img_dim,
+                      const void *gcf, size_t gcf_dim) {
+  gg_options o;
+  {
+    std::lock_guard<std::mutex> lk(g_opt_mu);
+    o = g_global_opts;
+  }
+  return gg_grid_host(&o, out_type, out, in_type, in, in_type, vals, npts, img_dim,
+                      gcf, gcf_dim);
+}
+
+extern "C" int gg_gridGPU_zz(double *out, const double *in, const double *in_vals,
+                             size_t npts, size_t img_dim, const double *gcf,
+                             size_t gcf_dim) {
+  return host_typed(GG_C128, out, GG_C128, in, in_vals, npts, img_dim, gcf, gcf_dim);
+}
+extern "C" int gg_gridGPU_zc(double *out, const float *in, const float *in_vals,
+                             size_t npts, size_t img_dim, const float *gcf,
+                             size_t gcf_dim) {
+  return host_typed(GG_C128, out, GG_C64, in, in_vals, npts, img_dim, gcf, gcf_dim);
+}
+extern "C" int gg_gridGPU_cc(float *out, const float *in, const float *in_vals,
+                             size_t npts, size_t img_dim, const float *gcf,
+                             size_t gcf_dim) {
+  return host_typed(GG_C64, out, GG_C64, in, in_vals, npts, img_dim, gcf, gcf_dim);
+}

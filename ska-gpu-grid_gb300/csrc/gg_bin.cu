@@ -1,0 +1,395 @@
+// Index step and uv-tile binning on the device.
+//
+// Replaces, for the binned methods, the reference's host-side qsort by uv tile
+// (comp_grid, grid.cu:256-276, dispatch grid.cu:467-475), vis2ints
+// (grid_gpu.cu:352-365) and set_bookmarks (grid_gpu.cu:366-390):
+//
+//   bin_count    index step per visibility (bit-exact with grid.cu:159-163),
+//                packed main*G+sub pair, global uv-tile key, tile histogram
+//   scan         exclusive prefix sum of the histogram = bookmarks
+//   bin_scatter  places every kept visibility at its sorted position and
+//                copies its packed indices and values there (SoA planes), so
+//                the gridding kernels stream each tile contiguously
+//
+// All kernels work on a batch of jobs sharing one global visibility index
+// space and one global tile space; a single job is a batch of one.
+#include <climits>
+
+#include "gg_common.cuh"
+#include "gg_internal.h"
+
+namespace gg {
+
+__device__ __forceinline__ int find_job64(const int64_t *base, int njobs,
+                                          int64_t g) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(base + mid) <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ int find_job32(const int *base, int njobs, int g) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(base + mid) <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// index step of visibility n of a uv array of either precision
+__device__ __forceinline__ bool uv_index(const void *uv, int uv_f64, int64_t n,
+                                         int G, int &mx, int &sx, int &my,
+                                         int &sy) {
+  if (uv_f64) {
+    double2 c = __ldg((const double2 *)uv + n);
+    bool a = index_step(c.x, G, mx, sx);
+    bool b = index_step(c.y, G, my, sy);
+    return a && b;
+  }
+  float2 c = __ldg((const float2 *)uv + n);
+  bool a = index_step(c.x, G, mx, sx);
+  bool b = index_step(c.y, G, my, sy);
+  return a && b;
+}
+
+__global__ void __launch_bounds__(256)
+    vis2ints_kernel(int uv_f64, const void *uv, int64_t npts, int G,
+                    int2 *packed, int *flags) {
+  for (int64_t n = blockIdx.x * 256ll + threadIdx.x; n < npts;
+       n += (int64_t)gridDim.x * 256) {
+    int mx, sx, my, sy;
+    if (uv_index(uv, uv_f64, n, G, mx, sx, my, sy)) {
+      packed[n] = make_int2(mx * G + sx, my * G + sy);
+    } else {
+      packed[n] = make_int2(INT_MIN, INT_MIN);
+      atomicAdd(&flags[FLAG_INDEX], 1);
+    }
+  }
+}
+
+// Pass 1.  Every visibility of every job: index step, drop rules, tile key,
+// warp-aggregated histogram increment.
+//  * a visibility whose oversample index falls outside [0,G) would address
+//    outside the GCF table in the reference; it is dropped and counted
+//  * a visibility whose footprint misses the grid contributes nothing and is
+//    dropped silently (the reference skips all of its taps, grid.cu:174-176)
+//  * mains left/right of the grid are clamped into the edge tile: all of
+//    their on-grid taps still lie inside that tile's window region
+__global__ void __launch_bounds__(256) bin_count_kernel(BinBuffers b) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * 256ll + (threadIdx.x & ~31);
+       base < b.total_vis; base += (int64_t)gridDim.x * 256) {
+    int64_t g = base + lane;
+    bool valid = g < b.total_vis;
+    int key = -1;
+    bool bad = false;
+    if (valid) {
+      int j = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, g);
+      const BinJob &J = b.jobs[j];
+      int mx, sx, my, sy;
+      int2 pk = make_int2(INT_MIN, INT_MIN);
+      bool ok = uv_index(J.uv, J.uv_f64, g - J.vis_base, J.G, mx, sx, my, sy);
+      if (ok && ((unsigned)sx >= (unsigned)J.G || (unsigned)sy >= (unsigned)J.G))
+        ok = false;
+      bad = !ok;
+      if (ok) {
+        pk = make_int2(mx * J.G + sx, my * J.G + sy);
+        const int h = J.S >> 1;
+        if (mx + h >= 0 && mx - h + 1 < J.N && my + h >= 0 && my - h + 1 < J.N) {
+          int cx = min(max(mx, 0), J.N - 1) >> J.log2T;
+          int cy = min(max(my, 0), J.N - 1) >> J.log2T;
+          key = J.tile_base + cy * J.ntx + cx;
+        }
+      }
+      b.packed[g] = pk;
+      b.key[g] = key;
+      if (b.kept_pos) b.kept_pos[g] = key >= 0 ? 1 : 0;
+    }
+    unsigned badm = __ballot_sync(0xffffffffu, bad);
+    if (badm && lane == 0) atomicAdd(&b.flags[FLAG_INDEX], __popc(badm));
+    unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && lane == __ffs(peers) - 1)
+      atomicAdd(&b.bookmarks[key], __popc(peers));
+  }
+}
+
+// Pass 3.  Sorted position of every kept visibility; copy of its packed
+// indices (and of its values, one plane per polarisation).
+//   generic:       position = bookmarks[key] + claim on cursor[key]
+//                  (one atomic per run of equal keys within a warp)
+//   input_sorted:  position = number of kept visibilities before it, which
+//                  keeps input order; a visibility landing outside its own
+//                  tile's range proves the input was not tile-sorted
+__global__ void __launch_bounds__(256) bin_scatter_kernel(BinBuffers b) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * 256ll + (threadIdx.x & ~31);
+       base < b.total_vis; base += (int64_t)gridDim.x * 256) {
+    int64_t g = base + lane;
+    bool valid = g < b.total_vis;
+    int key = valid ? b.key[g] : -1;
+    int pos = -1;
+    if (b.input_sorted) {
+      if (key >= 0) {
+        pos = b.kept_pos[g];
+        if (pos < b.bookmarks[key] || pos >= b.bookmarks[key + 1]) {
+          atomicOr(&b.flags[FLAG_UNSORTED], 1);
+          pos = -1;
+        }
+      }
+    } else {
+      unsigned peers = __match_any_sync(0xffffffffu, key);
+      int leader = __ffs(peers) - 1;
+      int start = 0;
+      if (key >= 0 && lane == leader)
+        start = atomicAdd(&b.cursor[key], __popc(peers));
+      start = __shfl_sync(0xffffffffu, start, leader);
+      if (key >= 0) pos = start + __popc(peers & lanemask_lt());
+    }
+    if (pos >= 0) {
+      b.sorted_idx[pos] = b.packed[g];
+      int j = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, g);
+      const BinJob &J = b.jobs[j];
+      int64_t n = g - J.vis_base;
+      if (b.vals_bytes == 8) {
+        const float2 *v = (const float2 *)J.vals + n * b.P;
+        float2 *o = (float2 *)b.sorted_vals;
+        for (int p = 0; p < b.P; ++p) o[p * b.vstride + pos] = __ldg(v + p);
+      } else {
+        const double2 *v = (const double2 *)J.vals + n * b.P;
+        double2 *o = (double2 *)b.sorted_vals;
+        for (int p = 0; p < b.P; ++p) o[p * b.vstride + pos] = __ldg(v + p);
+      }
+      if (b.order) b.order[pos] = (int)g;
+    }
+  }
+}
+
+// ---- exclusive scan ---------------------------------------------------------
+constexpr int kScanThreads = 256, kScanPer = 8,
+              kScanBlock = kScanThreads * kScanPer;
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_block_kernel(int *d, int64_t n, int *bsum) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int64_t base = blockIdx.x * (int64_t)kScanBlock + threadIdx.x * kScanPer;
+  int v[kScanPer];
+  if (base + kScanPer <= n) {
+    int4 a = *reinterpret_cast<const int4 *>(d + base);
+    int4 c = *reinterpret_cast<const int4 *>(d + base + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = c.x; v[5] = c.y; v[6] = c.z; v[7] = c.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < kScanPer; ++i) v[i] = base + i < n ? d[base + i] : 0;
+  }
+  int s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanPer; ++i) {
+    int t = v[i];
+    v[i] = s;
+    s += t;
+  }
+  int incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  __shared__ int wsum[kScanThreads / 32];
+  __shared__ int total;
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int x = lane < kScanThreads / 32 ? wsum[lane] : 0;
+    int xi = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += y;
+    }
+    if (lane < kScanThreads / 32) wsum[lane] = xi - x;
+    if (lane == 31) total = xi;
+  }
+  __syncthreads();
+  int off = wsum[warp] + incl - s;
+  if (base + kScanPer <= n) {
+    int4 a = make_int4(v[0] + off, v[1] + off, v[2] + off, v[3] + off);
+    int4 c = make_int4(v[4] + off, v[5] + off, v[6] + off, v[7] + off);
+    *reinterpret_cast<int4 *>(d + base) = a;
+    *reinterpret_cast<int4 *>(d + base + 4) = c;
+  } else {
+#pragma unroll
+    for (int i = 0; i < kScanPer; ++i)
+      if (base + i < n) d[base + i] = v[i] + off;
+  }
+  if (bsum && threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    scan_add_kernel(int *d, int64_t n, const int *boff) {
+  int add = boff[blockIdx.x];
+  int64_t base = blockIdx.x * (int64_t)kScanBlock;
+  for (int i = threadIdx.x; i < kScanBlock; i += kScanThreads)
+    if (base + i < n) d[base + i] += add;
+}
+
+static int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+size_t scan_tmp_ints(int64_t n) {
+  size_t t = 0;
+  while (n > kScanBlock) {
+    n = cdiv(n, kScanBlock);
+    t += (size_t)((n + 7) & ~7ll) + 8;
+  }
+  return t + 8;
+}
+
+cudaError_t scan_exclusive(int *d, int64_t n, int *tmp, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  int64_t nb = cdiv(n, kScanBlock);
+  scan_block_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(d, n, nb > 1 ? tmp : nullptr);
+  count_launch();
+  if (nb > 1) {
+    cudaError_t e = scan_exclusive(tmp, nb, tmp + ((nb + 7) & ~7ll) + 8, s);
+    if (e != cudaSuccess) return e;
+    scan_add_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(d, n, tmp);
+    count_launch();
+  }
+  return cudaGetLastError();
+}
+
+// ---- driver -----------------------------------------------------------------
+static unsigned grid_for(int64_t n) {
+  int64_t b = cdiv(n, 256);
+  return (unsigned)(b < 1 ? 1 : (b > 152 * 64 ? 152 * 64 : b));
+}
+
+cudaError_t launch_vis2ints(int uv_f64, const void *uv, int64_t npts, int G,
+                            int2 *packed, int *flags, cudaStream_t s) {
+  if (npts <= 0) return cudaSuccess;
+  vis2ints_kernel<<<grid_for(npts), 256, 0, s>>>(uv_f64, uv, npts, G, packed,
+                                                 flags);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t run_binning(const BinBuffers &b, cudaStream_t s) {
+  cudaError_t e;
+  e = cudaMemsetAsync(b.bookmarks, 0, sizeof(int) * (size_t)(b.total_tiles + 1), s);
+  if (e != cudaSuccess) return e;
+  if (b.total_vis > 0) {
+    bin_count_kernel<<<grid_for(b.total_vis), 256, 0, s>>>(b);
+    count_launch();
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = scan_exclusive(b.bookmarks, b.total_tiles + 1, b.scan_tmp, s)) != cudaSuccess)
+    return e;
+  if (b.input_sorted) {
+    if ((e = scan_exclusive(b.kept_pos, b.total_vis, b.scan_tmp, s)) != cudaSuccess)
+      return e;
+  } else {
+    e = cudaMemcpyAsync(b.cursor, b.bookmarks, sizeof(int) * (size_t)b.total_tiles,
+                        cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
+  if (b.total_vis > 0) {
+    bin_scatter_kernel<<<grid_for(b.total_vis), 256, 0, s>>>(b);
+    count_launch();
+  }
+  return cudaGetLastError();
+}
+
+// ---- work items ---------------------------------------------------------------
+constexpr int kMaxClasses = 4;
+
+__global__ void __launch_bounds__(256)
+    make_items_kernel(const int *bm, const int *tile_base, const int *job_class,
+                      int njobs, int total_tiles, int chunk, WorkItem *items,
+                      int64_t class_cap, int *counters) {
+  const int lane = threadIdx.x & 31;
+  for (int base = blockIdx.x * 256 + (threadIdx.x & ~31); base < total_tiles;
+       base += gridDim.x * 256) {
+    int t = base + lane;
+    int k = 0, s0 = 0, e0 = 0, j = 0, cls = 0;
+    if (t < total_tiles) {
+      s0 = bm[t];
+      e0 = bm[t + 1];
+      k = (e0 - s0 + chunk - 1) / chunk;
+      j = njobs == 1 ? 0 : find_job32(tile_base, njobs, t);
+      cls = job_class ? job_class[j] : 0;
+    }
+#pragma unroll
+    for (int c = 0; c < kMaxClasses; ++c) {
+      int kc = (cls == c) ? k : 0;
+      int incl = kc;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      int tot = __shfl_sync(0xffffffffu, incl, 31);
+      int start = 0;
+      if (lane == 0 && tot) start = atomicAdd(&counters[c], tot);
+      start = __shfl_sync(0xffffffffu, start, 0);
+      if (kc) {
+        WorkItem *dst = items + c * class_cap + start + (incl - kc);
+        int local = t - tile_base[j];
+        for (int i = 0; i < kc; ++i) {
+          WorkItem w;
+          w.job = j;
+          w.bin = local;
+          w.start = s0 + i * chunk;
+          w.end = min(e0, s0 + (i + 1) * chunk);
+          dst[i] = w;
+        }
+      }
+    }
+  }
+}
+
+cudaError_t launch_make_items(const int *bookmarks, const int *tile_base,
+                              const int *job_class, int njobs, int total_tiles,
+                              int chunk, WorkItem *items, int64_t class_cap,
+                              int *counters, cudaStream_t s) {
+  if (total_tiles <= 0) return cudaSuccess;
+  make_items_kernel<<<grid_for(total_tiles), 256, 0, s>>>(
+      bookmarks, tile_base, job_class, njobs, total_tiles, chunk, items,
+      class_cap, counters);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// ---- DEBUG1 footprint inputs --------------------------------------------------
+__global__ void count_inputs_kernel(void *vals, int vals_f64, int64_t npts,
+                                    int P, void *gcf, int64_t gcf_elems) {
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       i < npts * P; i += stride) {
+    int64_t n = i / P;
+    if (vals_f64) ((double2 *)vals)[i] = make_double2(1.0, (double)n);
+    else ((float2 *)vals)[i] = make_float2(1.f, (float)n);
+  }
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       i < gcf_elems; i += stride) {
+    if (vals_f64) ((double2 *)gcf)[i] = make_double2(1.0, 0.0);
+    else ((float2 *)gcf)[i] = make_float2(1.f, 0.f);
+  }
+}
+
+cudaError_t launch_count_inputs(void *vals, int vals_f64, int64_t npts, int P,
+                                void *gcf, int64_t gcf_elems, cudaStream_t s) {
+  count_inputs_kernel<<<grid_for(npts * P > gcf_elems ? npts * P : gcf_elems),
+                        256, 0, s>>>(vals, vals_f64, npts, P, gcf, gcf_elems);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace gg

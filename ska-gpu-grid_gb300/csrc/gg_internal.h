@@ -1,0 +1,109 @@
+// Host-side launcher interfaces between the C ABI (gg_api.cu) and the
+// kernel translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gg_types.h"
+
+namespace gg {
+
+// process-wide count of kernel launches made by the library
+void count_launch(int n = 1);
+
+// One job of a binning pass.  Visibilities of all jobs of a batch live in one
+// global index space: job j owns global indices [vis_base, vis_base+npts) and
+// global uv tiles [tile_base, tile_base+ntiles).
+struct BinJob {
+  const void *uv;
+  const void *vals;
+  int64_t vis_base;
+  int64_t npts;
+  int tile_base, ntiles;
+  int N, S, G, log2G, log2T, ntx, P;
+  int uv_f64;
+};
+
+struct BinBuffers {
+  const BinJob *jobs;      // device [njobs]
+  const int64_t *vis_base; // device [njobs+1]
+  const int *tile_base;    // device [njobs+1]
+  int njobs;
+  int64_t total_vis;       // sum of npts
+  int total_tiles;         // sum of ntiles
+  int vals_bytes;          // 8 (complex64) or 16 (complex128)
+  int P;                   // polarisations (uniform over the batch)
+  int2 *packed;            // [total_vis]
+  int *key;                // [total_vis] global tile id or -1 (dropped)
+  int *bookmarks;          // [total_tiles+1]: counts, then exclusive offsets
+  int *cursor;             // [total_tiles]
+  int *scan_tmp;           // scratch for the multi-level scan
+  int2 *sorted_idx;        // [total_vis + pad]
+  void *sorted_vals;       // [P][vstride]
+  int64_t vstride;
+  int *order;              // [total_vis] or null
+  int *flags;
+  int input_sorted;
+  int *kept_pos;           // [total_vis+1] (input_sorted only)
+};
+
+// index step only (vis2ints)
+cudaError_t launch_vis2ints(int uv_f64, const void *uv, int64_t npts, int G,
+                            int2 *packed, int *flags, cudaStream_t s);
+// count, scan, scatter; leaves bookmarks = exclusive offsets [total_tiles+1]
+cudaError_t run_binning(const BinBuffers &b, cudaStream_t s);
+// exclusive scan of n ints in place; tmp needs scan_tmp_ints(n) ints
+size_t scan_tmp_ints(int64_t n);
+cudaError_t scan_exclusive(int *data, int64_t n, int *tmp, cudaStream_t s);
+
+// Work items for the moving-window kernel: every non-empty tile of job j
+// (global tiles tile_base..) is cut into slices of at most `chunk` sorted
+// visibilities.  Items of jobs of S-class c go to items + c*class_cap,
+// counted in counters[c].
+cudaError_t launch_make_items(const int *bookmarks, const int *tile_base,
+                              const int *job_class, int njobs,
+                              int total_tiles, int chunk, WorkItem *items,
+                              int64_t class_cap, int *counters,
+                              cudaStream_t s);
+
+// ---- gridding launches ----------------------------------------------------
+struct GridLaunch {
+  const JobDesc *jobs;     // device [njobs]
+  int njobs;
+  int S;                   // support of every job in this launch
+  int accum;               // GG_ACC_*
+  int vals_f64;
+  int gauss;
+  float sigma;             // GAUSS: uniform over the launch
+  int G;                   // oversampling, uniform over the launch
+  int tile;                // uv tile side, uniform over the launch
+  int P;
+  int *flags;
+  int sm_count;
+  // scatter: global visibility space
+  const int64_t *vis_base; // device [njobs+1]
+  int64_t total_vis;
+  // window: work queue
+  const WorkItem *items;
+  const int *nitems;
+  int *item_next;
+  int64_t max_items;
+  // gather: global tiles of the jobs in this launch
+  const int *tile_base;    // device [njobs+1]
+  int total_tiles;
+};
+
+cudaError_t launch_scatter(const GridLaunch &g, cudaStream_t s);
+cudaError_t launch_window(const GridLaunch &g, cudaStream_t s);
+cudaError_t launch_gather(const GridLaunch &g, cudaStream_t s);
+// compensated scatter with complex64 output: out = fl(hi + lo)
+cudaError_t launch_comp_finalize(float *out, const float *lo, int64_t n,
+                                 cudaStream_t s);
+// substitute inputs of the DEBUG1 footprint mode: vals[n*P+p] = (1, n),
+// gcf = (1, 0) everywhere
+cudaError_t launch_count_inputs(void *vals, int vals_f64, int64_t npts, int P,
+                                void *gcf, int64_t gcf_elems, cudaStream_t s);
+// smem bytes the window kernel needs (for occupancy sizing)
+size_t window_smem_bytes(int S, int accum, int vals_f64);
+
+}  // namespace gg

@@ -1,0 +1,86 @@
+// Pieces shared by the three gridding kernels.
+#pragma once
+#include "gg_common.cuh"
+#include "gg_internal.h"
+
+namespace gg {
+
+// Per-launch parameters every gridding kernel receives by value.
+struct KParams {
+  const JobDesc *jobs;
+  const WorkItem *items;
+  const int *nitems;
+  int *item_next;
+  int *flags;
+  const int64_t *vis_base;
+  const int *tile_base;
+  int64_t total_vis;
+  int njobs;
+  int total_tiles;
+  int P;
+  int T;        // uv tile side, uniform within a launch
+  int G;        // oversampling, uniform within a launch
+  float sigma;  // GAUSS sigma, uniform within a launch
+};
+
+// GCF value of tap (a', b') of sub-kernel (sx, sy)
+template <int S, bool GAUSS, typename VT>
+struct GcfSrc;
+
+// tabulated: the reference's [G*G][S][S] layout (grid.cu:169-172)
+template <int S, typename VT>
+struct GcfSrc<S, false, VT> {
+  using VT2 = typename vec2_of<VT>::type;
+  const VT2 *tab;
+  int G;
+  __device__ __forceinline__ void value(int sx, int sy, int ap, int bp, VT &gr,
+                                        VT &gi) const {
+    VT2 g = __ldg(tab + ((size_t)(sy * G + sx) * S + bp) * S + ap);
+    gr = g.x;
+    gi = g.y;
+  }
+};
+
+// COMPUTE_GCF: separable Gaussian from per-CTA 1-D factors g1[s*S + a'],
+// evaluated in the prologue with expf (real, imaginary part zero)
+template <int S, typename VT>
+struct GcfSrc<S, true, VT> {
+  const float *g1;
+  __device__ __forceinline__ void value(int sx, int sy, int ap, int bp, VT &gr,
+                                        VT &gi) const {
+    gr = (VT)(g1[sx * S + ap] * g1[sy * S + bp]);
+    gi = (VT)0;
+  }
+};
+
+// g1[s][a'] = exp(-(a' - S/2 + 1 - s/G)^2 / (2 sigma^2)) in FP32
+__device__ __forceinline__ void gauss_fill(float *g1, int S, int G, float sigma,
+                                           int tid, int nt) {
+  const float inv = 1.0f / (2.0f * sigma * sigma);
+  for (int i = tid; i < G * S; i += nt) {
+    int s = i / S, ap = i % S;
+    float x = (float)(ap - S / 2 + 1) - (float)s / (float)G;
+    g1[i] = expf(-(x * x) * inv);
+  }
+}
+
+// Adds a finished cell value into the output grid (type from the job)
+__device__ __forceinline__ void out_red(const JobDesc &J, size_t cell, int p,
+                                        int P, double re, double im) {
+  size_t NN = (size_t)J.N * J.N;
+  if (J.out_f64) grid_red<double>((double *)J.out, cell, p, P, NN, J.planar, re, im);
+  else grid_red<float>((float *)J.out, cell, p, P, NN, J.planar, re, im);
+}
+
+template <class ACC>
+__device__ __forceinline__ void out_red_acc(const JobDesc &J, size_t cell,
+                                            int p, int P, const ACC &a) {
+  size_t NN = (size_t)J.N * J.N;
+  if (J.out_f64)
+    grid_red<double>((double *)J.out, cell, p, P, NN, J.planar, a.dre(), a.dim());
+  else
+    grid_red<float>((float *)J.out, cell, p, P, NN, J.planar, (double)a.fre(),
+                    (double)a.fim());
+}
+
+}  // namespace gg

@@ -1,0 +1,48 @@
+// Internal types shared by the host launchers and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gg.h"
+
+namespace gg {
+
+// device flag slots (context-owned int32[8]); see gg_read_flags
+enum { FLAG_INDEX = 0, FLAG_TIMEOUT = 1, FLAG_UNSORTED = 2, FLAG_BOUNDS = 3 };
+
+constexpr int kMaxPols = 8;
+constexpr int kBinThreads = 256;
+
+// One gridding job as the kernels see it.  For the binned methods `idx` and
+// `vals` are the tile-sorted copies made by the binning pass: idx[k] is the
+// packed (main*G+sub) pair of sorted visibility k and vals holds P planes of
+// `vstride` complex values each.  Scatter reads the caller's uv/vals.
+struct JobDesc {
+  void *out;             // grid head (N*N*P complex of out type)
+  const void *uv;        // caller's (u,v), scatter only
+  const void *vals;      // values: sorted planes (binned) or caller's (scatter)
+  const int2 *idx;       // sorted packed indices (binned)
+  const void *gcf;       // un-offset table [G*G][S][S] (TABLE)
+  const int *bookmarks;  // [ntiles+1] sorted offsets per uv tile (binned)
+  float *lo;             // FP32 lo grid for compensated scatter (or null)
+  int64_t npts;          // visibilities (scatter) / kept (binned)
+  int64_t vstride;       // plane stride of sorted vals
+  int N, S, G, log2G, P, T, log2T, ntx;
+  int planar, out_f64, uv_f64;
+  float sigma;
+};
+
+// A slice of one uv tile's sorted visibilities: the unit of the device work
+// queue of the moving-window kernel (and of batched launches).
+struct WorkItem {
+  int job;
+  int bin;
+  int start;
+  int end;
+};
+
+template <typename T> struct vec2_of;
+template <> struct vec2_of<float> { using type = float2; };
+template <> struct vec2_of<double> { using type = double2; };
+
+}  // namespace gg

@@ -1,0 +1,137 @@
+"""Seeded synthetic visibilities with the shapes of the benchmark workloads.
+
+No public dataset exists for this path; these generators stand in for it.
+Coordinates are FP64 grid-pixel positions rounded to float32-representable
+values, the convention of the reference harness (grid.cu:446, computed in
+float), under which the cell/oversample index step is exact on every path.
+
+* ``uniform``  -- u,v uniform in [lo, hi) (plain-scatter workload: 1024^2,
+                  2^18 visibilities, support 16)
+* ``tracks``   -- realistic uv tracks: antennas uniform in a disk, all
+                  baselines, hour-angle samples at a declination, scaled to
+                  fill a fraction of the grid (gather / moving-window
+                  workload: 4096^2, 64 antennas, 2016 baselines x 2080 samples
+                  over +-4 h at dec -30 deg, 90% fill, padded to 2^22)
+* ``disk``     -- uniform density in a disk, N(0,1) values with a fraction of
+                  outliers (precision workload: 8192^2, 2^24, 1% at 1e3)
+* ``gaussian_gcf`` -- the separable Gaussian table, sigma = S/4
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def fr(a) -> np.ndarray:
+    """float32-representable float64"""
+    return np.asarray(a, np.float32).astype(np.float64)
+
+
+def normal_vals(rng, n: int, dtype=np.complex64, outlier_frac: float = 0.0,
+                outlier_amp: float = 1e3) -> np.ndarray:
+    v = (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    if outlier_frac > 0:
+        k = int(round(n * outlier_frac))
+        idx = rng.choice(n, size=k, replace=False)
+        ph = rng.uniform(0, 2 * np.pi, size=k)
+        v[idx] = outlier_amp * np.exp(1j * ph)
+    return v.astype(dtype)
+
+
+def uniform(npts: int, lo: float, hi: float, seed: int = 0,
+            vals_dtype=np.complex64, pols: int = 1):
+    rng = np.random.default_rng(seed)
+    uv = fr(rng.uniform(lo, hi, size=(npts, 2)))
+    vals = normal_vals(rng, npts * pols, vals_dtype)
+    return uv, vals
+
+
+def _antennas(rng, nant: int, radius_m: float) -> np.ndarray:
+    r = radius_m * np.sqrt(rng.uniform(0, 1, nant))
+    th = rng.uniform(0, 2 * np.pi, nant)
+    return np.stack([r * np.cos(th), r * np.sin(th), np.zeros(nant)], axis=1)
+
+
+def tracks(img_dim: int = 4096, nant: int = 64, ntime: int = 2080,
+           ha_hours: float = 4.0, dec_deg: float = -30.0, fill: float = 0.9,
+           radius_m: float = 1000.0, npts: int | None = 1 << 22,
+           seed: int = 0, vals_dtype=np.complex64):
+    """uv tracks of all nant*(nant-1)/2 baselines over hour angles
+    [-ha, ha]; (u,v) in pixels centred at img_dim/2, the longest projected
+    baseline at fill*img_dim/2.  Visibilities are baseline-major, time-minor;
+    when npts exceeds nbl*ntime the first baselines get extra samples past
+    the end of the track, when it is smaller the tail is cut."""
+    rng = np.random.default_rng(seed)
+    ant = _antennas(rng, nant, radius_m)
+    i, j = np.triu_indices(nant, k=1)
+    bl = ant[j] - ant[i]                                  # (nbl, 3) metres
+    nbl = bl.shape[0]
+    total = nbl * ntime if npts is None else npts
+    extra = max(0, total - nbl * ntime)
+    ha = np.linspace(-ha_hours, ha_hours, ntime) * (np.pi / 12.0)
+    dha = ha[1] - ha[0] if ntime > 1 else 0.0
+    dec = math.radians(dec_deg)
+    sd, cd = math.sin(dec), math.cos(dec)
+
+    def uvw(b, h):
+        sh, ch = np.sin(h), np.cos(h)
+        u = sh * b[..., 0] + ch * b[..., 1]
+        v = -sd * ch * b[..., 0] + sd * sh * b[..., 1] + cd * b[..., 2]
+        return u, v
+
+    u, v = uvw(bl[:, None, :], ha[None, :])               # (nbl, ntime)
+    u, v = u.reshape(-1), v.reshape(-1)
+    if extra:
+        k = np.arange(extra)
+        b = bl[k % nbl]
+        h = ha[-1] + dha * (1 + k // nbl)
+        ue, ve = uvw(b, h)
+        u, v = np.concatenate([u, ue]), np.concatenate([v, ve])
+    u, v = u[:total], v[:total]
+    scale = fill * (img_dim / 2) / max(np.abs(u).max(), np.abs(v).max())
+    uv = fr(np.stack([img_dim / 2 + u * scale, img_dim / 2 + v * scale], axis=1))
+    vals = normal_vals(rng, total, vals_dtype)
+    return uv, vals
+
+
+def disk(npts: int, img_dim: int, fill: float = 0.9, seed: int = 0,
+         outlier_frac: float = 0.0, outlier_amp: float = 1e3,
+         vals_dtype=np.complex64):
+    rng = np.random.default_rng(seed)
+    r = fill * (img_dim / 2) * np.sqrt(rng.uniform(0, 1, npts))
+    th = rng.uniform(0, 2 * np.pi, npts)
+    uv = fr(np.stack([img_dim / 2 + r * np.cos(th),
+                      img_dim / 2 + r * np.sin(th)], axis=1))
+    vals = normal_vals(rng, npts, vals_dtype, outlier_frac, outlier_amp)
+    return uv, vals
+
+
+def tile_sort(uv: np.ndarray, img_dim: int, tile: int = 32, gcf_dim: int = 8,
+              oversample: int = 8):
+    """Stable order grouping visibilities by uv tile (of the main cell,
+    clamped into the grid as the device binning does); returns the
+    permutation."""
+    m = np.floor(uv).astype(np.int64)
+    m = np.clip(m, 0, img_dim - 1)
+    ntx = (img_dim + tile - 1) // tile
+    key = (m[:, 1] // tile) * ntx + (m[:, 0] // tile)
+    return np.argsort(key, kind="stable")
+
+
+def gaussian_gcf_1d(gcf_dim: int, oversample: int = 8,
+                    sigma: float | None = None) -> np.ndarray:
+    """[G][S] factors g(a' - S/2 + 1 - s/G), g(x) = exp(-x^2 / (2 sigma^2))"""
+    if sigma is None:
+        sigma = gcf_dim / 4.0
+    s = np.arange(oversample)[:, None]
+    a = np.arange(gcf_dim)[None, :]
+    x = (a - gcf_dim // 2 + 1) - s / oversample
+    return np.exp(-(x * x) / (2.0 * sigma * sigma))
+
+
+def gcf_table(g1: np.ndarray) -> np.ndarray:
+    """complex128 [G*G, S, S] table from 1-D factors (exact products)."""
+    G, S = g1.shape
+    t = g1[None, :, None, :] * g1[:, None, :, None]       # [sy, sx, b', a']
+    return t.reshape(G * G, S, S).astype(np.complex128)

@@ -1,0 +1,403 @@
+"""GPU parity of the CUDA gridder against the CPU oracle (gridCPU_pz
+restatement pinned to the reference's own output) -- all calls go through
+the C ABI of libgg.so.
+
+Tolerances (normwise: max |gpu - oracle| / max |oracle|):
+  FP64 values, complex128 grid ............................ 1e-12
+  FP32 values, compensated (two-sum hi/lo) accumulation ..... 1e-6
+  FP32 values, plain FP32 accumulation ...................... 2e-6
+  on-the-fly Gaussian GCF (FP32 expf vs FP64 table) ......... 1e-6
+Index work (cell and oversample index, DEBUG1 footprints, bookmarks) is
+compared bit-exactly.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import gpugrid as gg
+import oracle as O
+import synth
+from helpers import GOLDEN_CASES, load_golden, planar_from_grid, rel_err, to_complex
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+TOL = {"zz": 1e-12, "zc": 1e-6, "cc": 2e-6, "cc_comp": 1e-6}
+MODES = {"scatter": gg.MODE_SCATTER, "gather": gg.MODE_GATHER, "window": gg.MODE_WINDOW}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    c = gg.Context(0)
+    yield c
+    c.close()
+
+
+def run(ctx, opts, uv, vals, gcf, N, S, prec, uv_dtype=np.float64, stream=None):
+    """Grid on the device; returns (planar float64 grid (2,P,N,N), flags)."""
+    vdt = np.complex128 if prec == "zz" else np.complex64
+    odt = torch.complex64 if prec.startswith("cc") else torch.complex128
+    P = opts.polarizations
+    d_uv = torch.from_numpy(np.ascontiguousarray(uv, uv_dtype)).cuda()
+    d_vals = torch.from_numpy(np.ascontiguousarray(vals, vdt)).cuda()
+    d_gcf = (torch.from_numpy(np.ascontiguousarray(gcf, vdt).reshape(-1)).cuda()
+             if gcf is not None else None)
+    out = torch.full((P * N * N,), float("nan"), dtype=odt, device="cuda")
+    ctx.grid(opts, out, d_uv, d_vals, d_gcf, N, S)
+    torch.cuda.synchronize()
+    flags = ctx.read_flags()
+    planar = opts.layout == gg.LAYOUT_PLANAR or (
+        opts.layout == gg.LAYOUT_REFERENCE and opts.mode == gg.MODE_WINDOW)
+    host = torch.view_as_real(out).reshape(-1).cpu().numpy()
+    return planar_from_grid(host, P, N, planar), flags
+
+
+def oracle_for(uv, vals, gcf, N, S, P=1, G=8, debug1=False):
+    """oracle on exactly the values the GPU saw (vals/gcf complex arrays)"""
+    return O.grid_pz(uv, to_pairs(vals), to_pairs(gcf), N, S, pols=P, gcf_grid=G,
+                     debug1=debug1, nthreads=8)
+
+
+def to_pairs(c):
+    c = np.asarray(c).reshape(-1)
+    return np.stack([c.real, c.imag], -1).astype(np.float64)
+
+
+def opts_for(mode, prec, **kw):
+    acc = gg.ACC_COMPENSATED if prec in ("zc", "cc_comp") else gg.ACC_PLAIN
+    return gg.Options(mode=MODES[mode], accum=acc, **kw)
+
+
+# ---------------------------------------------------------------------------
+# golden fixtures (the reference's own output) -- every method and precision
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("prec", ["zz", "zc", "cc", "cc_comp"])
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if not c.startswith("debug1")])
+def test_golden(ctx, name, mode, prec):
+    g = load_golden(name)
+    N, S, P = g["N"], g["S"], g["P"]
+    vals = to_complex(g["vals"])
+    gcf = to_complex(g["gcf"])
+    if prec != "zz":
+        vals = vals.astype(np.complex64)
+        gcf = gcf.astype(np.complex64)
+    out, flags = run(ctx, opts_for(mode, prec, polarizations=P), g["uv"], vals, gcf, N, S, prec)
+    assert flags == [0, 0, 0, 0]
+    if prec == "zz":
+        assert rel_err(out, g["out"]) <= TOL["zz"]
+    else:
+        ref = oracle_for(g["uv"], vals, gcf, N, S, P)
+        assert rel_err(out, ref) <= TOL[prec], rel_err(out, ref)
+
+
+@pytest.mark.parametrize("prec", ["zz", "cc_comp", "cc"])
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+def test_debug1_footprint_bit_exact(ctx, mode, prec):
+    """DEBUG1 (Defines.h:78): every tap adds (1, visibility index); the grid
+    holds hit counts and index sums, exact integers in FP32 and FP64."""
+    g = load_golden("debug1_n64_s8")
+    N, S = g["N"], g["S"]
+    o = opts_for(mode, prec, gcf_kind=gg.GCF_COUNT)
+    vals = np.zeros(len(g["uv"]), np.complex128)
+    out, flags = run(ctx, o, g["uv"], vals, None, N, S, prec)
+    assert flags == [0, 0, 0, 0]
+    assert np.array_equal(out, g["out"])
+
+
+# ---------------------------------------------------------------------------
+# index step and binning (bit-exact)
+# ---------------------------------------------------------------------------
+def test_vis2ints_bit_exact_fp64(ctx):
+    rng = np.random.default_rng(7)
+    uv = rng.uniform(-40, 9000, size=(200000, 2))
+    uv[:100000] = uv[:100000].astype(np.float32)  # half float-representable
+    k = np.arange(1, 2001, dtype=np.float64)
+    uv[-2000:, 0] = k - 1e-9                           # just below integers
+    uv[-2000:, 1] = k + 1e-9
+    d = torch.from_numpy(uv).cuda()
+    got = gg.vis2ints(d).cpu().numpy()
+    assert np.array_equal(got, O.vis2ints(uv))
+
+
+def test_vis2ints_bit_exact_fp32(ctx):
+    rng = np.random.default_rng(8)
+    uv32 = rng.uniform(-100, 30000, size=(100000, 2)).astype(np.float32)
+    got = gg.vis2ints(torch.from_numpy(uv32).cuda()).cpu().numpy()
+    assert np.array_equal(got, O.vis2ints(uv32.astype(np.float64)))
+
+
+@pytest.mark.parametrize("input_sorted", [False, True])
+def test_bin_bookmarks(ctx, input_sorted):
+    N, S, T = 512, 8, 32
+    uv, _ = synth.uniform(30000, 0, N, seed=9)
+    if input_sorted:
+        uv = uv[synth.tile_sort(uv, N, T)]
+    o = gg.Options(tile=T, input_sorted=input_sorted)
+    bm, order = ctx.bin(o, torch.from_numpy(uv).cuda(), N, S)
+    bm, order = bm.cpu().numpy(), order.cpu().numpy()
+    pk = O.vis2ints(uv)
+    tile = (pk[:, 1] // 8 // T) * (N // T) + pk[:, 0] // 8 // T
+    srt = np.argsort(tile, kind="stable")
+    expect = O.set_bookmarks(pk[srt], T, N // T)
+    assert np.array_equal(bm, expect)
+    kept = bm[-1]
+    assert kept == len(uv)
+    assert np.array_equal(np.sort(order[:kept]), np.arange(len(uv)))
+    assert np.array_equal(tile[order[:kept]], np.sort(tile))
+    if input_sorted:
+        assert np.array_equal(order[:kept], np.arange(len(uv)))
+    assert ctx.read_flags() == [0, 0, 0, 0]
+
+
+def test_unsorted_input_detected(ctx):
+    N, S = 256, 8
+    uv, vals = synth.uniform(5000, 0, N, seed=10)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    out = np.zeros(gg.padded_size(N, S), np.complex64)
+    o = gg.Options(mode=gg.MODE_WINDOW, input_sorted=True)
+    with pytest.raises(gg.GridError) as e:
+        gg.grid_host(o, out, uv.astype(np.float32).view(np.complex64).reshape(-1).copy(),
+                     vals, len(uv), N, gcf, S)
+    assert e.value.code == gg.ERR_UNSORTED
+
+
+def test_out_of_table_index_dropped_and_counted(ctx):
+    """u right below an integer is not float-representable: the CPU gridder's
+    oversample index becomes -1 (outside its table); the GPU path drops the
+    visibility and counts it instead of reading outside the table."""
+    N, S = 64, 8
+    uv = np.array([[20.5, 20.5], [30.0 - 1e-9, 30.25], [40.5, 40.5]])
+    vals = np.ones(3, np.complex128)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S))
+    for mode in MODES:
+        out, flags = run(ctx, opts_for(mode, "zz"), uv, vals, gcf, N, S, "zz")
+        assert flags[0] == 1
+        ref = oracle_for(uv[[0, 2]], vals[[0, 2]], gcf, N, S)
+        assert rel_err(out, ref) <= 1e-12
+
+
+# ---------------------------------------------------------------------------
+# edge cases
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+def test_empty_and_offgrid_inputs_give_zero_grid(ctx, mode):
+    N, S = 96, 8
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    for uv in (np.zeros((0, 2)), np.array([[-10.0, 5.0], [200.0, 3.0], [5.0, 104.5]])):
+        vals = np.ones(len(uv), np.complex64)
+        out, flags = run(ctx, opts_for(mode, "cc_comp"), uv, vals, gcf, N, S, "cc_comp")
+        assert flags == [0, 0, 0, 0]
+        assert np.array_equal(out, np.zeros_like(out))
+
+
+@pytest.mark.parametrize("S", [4, 8, 16, 32])
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+def test_supports_and_ragged_grid(ctx, mode, S):
+    N = 100  # not a multiple of the 32-cell tile
+    uv, vals = synth.uniform(3000, -S, N + S, seed=S)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    out, flags = run(ctx, opts_for(mode, "cc_comp"), uv, vals, gcf, N, S, "cc_comp")
+    assert flags == [0, 0, 0, 0]
+    assert rel_err(out, oracle_for(uv, vals, gcf, N, S)) <= TOL["cc_comp"]
+
+
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+def test_corners_and_single_visibility(ctx, mode):
+    N, S = 64, 16
+    uv = np.array([[0.0, 0.0], [63.875, 63.875], [0.5, 63.5], [63.5, 0.25], [31.0, 32.0]])
+    vals = np.array([1 + 2j, -3 + 1j, 0.5 - 0.5j, 2j, 1], np.complex128)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S))
+    out, _ = run(ctx, opts_for(mode, "zz"), uv, vals, gcf, N, S, "zz")
+    assert rel_err(out, oracle_for(uv, vals, gcf, N, S)) <= 1e-12
+    for k in range(len(uv)):
+        out, _ = run(ctx, opts_for(mode, "zz"), uv[k:k + 1], vals[k:k + 1], gcf, N, S, "zz")
+        assert rel_err(out, oracle_for(uv[k:k + 1], vals[k:k + 1], gcf, N, S)) <= 1e-12
+
+
+@pytest.mark.parametrize("G", [1, 4, 16])
+def test_other_oversampling(ctx, G):
+    N, S = 128, 8
+    uv, vals = synth.uniform(4000, 0, N, seed=G)
+    g1 = synth.gaussian_gcf_1d(S, oversample=G)
+    gcf = synth.gcf_table(g1)
+    for mode in MODES:
+        out, _ = run(ctx, opts_for(mode, "zz", oversample=G), uv,
+                     vals.astype(np.complex128), gcf, N, S, "zz")
+        assert rel_err(out, oracle_for(uv, vals, gcf, N, S, G=G)) <= 1e-12
+
+
+@pytest.mark.parametrize("layout", [gg.LAYOUT_INTERLEAVED, gg.LAYOUT_PLANAR])
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+def test_layouts_and_float_coordinates(ctx, mode, layout):
+    N, S = 128, 8
+    uv, vals = synth.uniform(5000, 0, N, seed=11)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    o = opts_for(mode, "cc_comp", layout=layout)
+    out, _ = run(ctx, o, uv, vals, gcf, N, S, "cc_comp", uv_dtype=np.float32)
+    assert rel_err(out, oracle_for(uv, vals, gcf, N, S)) <= TOL["cc_comp"]
+
+
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+def test_gaussian_on_the_fly(ctx, mode):
+    """COMPUTE_GCF: the GPU evaluates the separable Gaussian in FP32; the
+    oracle gets the FP64 table of the same function."""
+    for N, S in ((128, 8), (128, 32)):
+        uv, vals = synth.uniform(6000, 0, N, seed=S)
+        gcf = synth.gcf_table(synth.gaussian_gcf_1d(S))
+        o = opts_for(mode, "cc_comp", gcf_kind=gg.GCF_GAUSSIAN)
+        out, _ = run(ctx, o, uv, vals, None, N, S, "cc_comp")
+        assert rel_err(out, oracle_for(uv, vals, gcf, N, S)) <= 1e-6
+
+
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+def test_output_is_overwritten_not_accumulated(ctx, mode):
+    N, S = 64, 8
+    uv, vals = synth.uniform(500, 0, N, seed=12)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    a, _ = run(ctx, opts_for(mode, "cc"), uv, vals, gcf, N, S, "cc")
+    b, _ = run(ctx, opts_for(mode, "cc"), uv, vals, gcf, N, S, "cc")
+    assert np.isfinite(a).all() and np.allclose(a, b, rtol=0, atol=1e-6 * np.abs(a).max())
+
+
+# ---------------------------------------------------------------------------
+# batches of jobs
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+def test_batch_equals_single_jobs(ctx, mode):
+    rng = np.random.default_rng(13)
+    specs = [(64, 8, 300), (256, 16, 5000), (96, 8, 0), (128, 16, 2000), (512, 8, 20000)]
+    o = opts_for(mode, "cc_comp")
+    jobs, keep, refs = [], [], []
+    for k, (N, S, n) in enumerate(specs):
+        uv, vals = synth.uniform(n, -S, N + S, seed=100 + k)
+        gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+        d = [torch.from_numpy(uv).cuda(), torch.from_numpy(vals).cuda(),
+             torch.from_numpy(gcf.reshape(-1)).cuda(),
+             torch.full((N * N,), float("nan"), dtype=torch.complex64, device="cuda")]
+        keep.append(d)
+        jobs.append(gg.Context.make_job(d[3], d[0], d[1], d[2], N, S, npts=n))
+        refs.append(oracle_for(uv, vals, gcf, N, S))
+    ctx.grid_batch(o, jobs)
+    torch.cuda.synchronize()
+    assert ctx.read_flags() == [0, 0, 0, 0]
+    for (N, S, n), d, ref in zip(specs, keep, refs):
+        host = torch.view_as_real(d[3]).reshape(-1).cpu().numpy()
+        out = planar_from_grid(host, 1, N, mode == "window")
+        assert rel_err(out, ref) <= TOL["cc_comp"]
+
+
+# ---------------------------------------------------------------------------
+# drop-in host entry points (padded buffers, reference semantics)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+@pytest.mark.parametrize("inst", ["zz", "zc", "cc"])
+def test_gridGPU_dropin_padded(ctx, mode, inst):
+    g = load_golden("gauss_n128_s16")
+    N, S = g["N"], g["S"]
+    it = np.complex128 if inst == "zz" else np.complex64
+    ot = np.complex64 if inst == "cc" else np.complex128
+    gg.set_global_options(gg.Options(mode=MODES[mode],
+                                     accum=gg.ACC_COMPENSATED if inst != "zz" else gg.ACC_PLAIN))
+    try:
+        uvc = np.ascontiguousarray(to_complex(g["uv"]).astype(it))
+        vals = np.ascontiguousarray(to_complex(g["vals"]).astype(it))
+        gcf = np.ascontiguousarray(to_complex(g["gcf"]).astype(it))
+        out = np.full(gg.padded_size(N, S), 7 + 7j, ot)
+        gg.gridGPU(out, uvc, vals, len(uvc), N, gcf, S)
+    finally:
+        gg.set_global_options(gg.Options())
+    h = gg.grid_head(N, S)
+    assert np.all(out[:h] == 0) and np.all(out[h + N * N:] == 0)
+    head = out[h:h + N * N]
+    if mode == "window":   # planar, like grid_kernel_window (grid_gpu.cu:524-525)
+        r = head.view(np.float64 if ot == np.complex128 else np.float32)
+        grid = np.stack([r[:N * N], r[N * N:]]).reshape(2, 1, N, N)
+    else:
+        grid = np.stack([head.real, head.imag]).reshape(2, 1, N, N)
+    if inst == "zz":
+        assert rel_err(grid, g["out"]) <= 1e-12
+    else:
+        ref = oracle_for(g["uv"].astype(np.float32).astype(np.float64), vals, gcf, N, S)
+        assert rel_err(grid, ref) <= 1e-6
+
+
+def test_convgrid_python3(ctx):
+    g = load_golden("gauss_n64_s8")
+    N, S = g["N"], g["S"]
+    flat_uv = g["uv"].reshape(-1).tolist()
+    vals = list(to_complex(g["vals"]))
+    gcf = list(to_complex(g["gcf"]))
+    grid = gg.convgrid(flat_uv, len(g["uv"]), vals, N, gcf, 8, S)
+    assert grid.shape == (N, N)
+    ref = g["out"][0, 0] + 1j * g["out"][1, 0]
+    assert np.abs(grid - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+# ---------------------------------------------------------------------------
+# full-size workloads: size-independent properties
+# ---------------------------------------------------------------------------
+def _device_inputs(uv, vals, gcf):
+    return (torch.from_numpy(uv).cuda(), torch.from_numpy(vals).cuda(),
+            torch.from_numpy(gcf.reshape(-1)).cuda())
+
+
+def test_tracks_4096_all_methods_agree_and_match_oracle_sample(ctx):
+    """gather / moving-window workload (4096^2, 2^22 visibilities on uv
+    tracks, S=8): the three methods agree; a 1/16 sample of the visibilities
+    is checked against the oracle."""
+    N, S = 4096, 8
+    uv, vals = synth.tracks(N, npts=1 << 22, seed=21)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    d_uv, d_vals, d_gcf = _device_inputs(uv, vals, gcf)
+    outs = {}
+    for mode in MODES:
+        o = opts_for(mode, "cc_comp", layout=gg.LAYOUT_INTERLEAVED)
+        out = torch.empty(N * N, dtype=torch.complex64, device="cuda")
+        ctx.grid(o, out, d_uv, d_vals, d_gcf, N, S)
+        outs[mode] = out
+    torch.cuda.synchronize()
+    ref = outs["window"]
+    scale = ref.abs().max().item()
+    for mode in ("scatter", "gather"):
+        assert (outs[mode] - ref).abs().max().item() <= 1e-6 * scale
+    sub = slice(0, None, 16)
+    o = opts_for("window", "cc_comp", layout=gg.LAYOUT_INTERLEAVED)
+    out = torch.empty(N * N, dtype=torch.complex64, device="cuda")
+    ctx.grid(o, out, *_device_inputs(np.ascontiguousarray(uv[sub]),
+                                     np.ascontiguousarray(vals[sub]), gcf), N, S)
+    host = torch.view_as_real(out).reshape(-1).cpu().numpy()
+    got = planar_from_grid(host, 1, N, False)
+    want = oracle_for(uv[sub], vals[sub], gcf, N, S)
+    assert rel_err(got, want) <= 1e-6
+
+
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+def test_linearity_and_checksum_large(ctx, mode):
+    """grid(a*v1 + b*v2) = a*grid(v1) + b*grid(v2), and the grid sum equals
+    sum_n v_n * (sum of the visibility's GCF taps) for on-grid footprints."""
+    N, S = 2048, 16
+    rng = np.random.default_rng(22)
+    uv, v1 = synth.disk(1 << 20, N, seed=22)
+    v2 = synth.normal_vals(rng, len(uv))
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    o = opts_for(mode, "cc_comp", layout=gg.LAYOUT_INTERLEAVED)
+    res = []
+    for v in (v1, v2, (2 * v1.astype(np.complex128) - 3 * v2).astype(np.complex64)):
+        out = torch.empty(N * N, dtype=torch.complex128, device="cuda")
+        d_uv, d_v, d_g = _device_inputs(uv, v, gcf)
+        ctx.grid(o, out, d_uv, d_v, d_g, N, S)
+        res.append(out)
+    torch.cuda.synchronize()
+    a, b, c = (r.cpu().numpy() for r in res)
+    lin = 2 * a - 3 * b
+    assert np.abs(c - lin).max() <= 1e-6 * np.abs(c).max()
+    pk = O.vis2ints(uv)
+    sx, sy = pk[:, 0] % 8, pk[:, 1] % 8
+    tapsum = gcf.reshape(64, S, S).sum(axis=(1, 2)).astype(np.complex128)
+    expect = (v1.astype(np.complex128) * tapsum[sy * 8 + sx]).sum()
+    bound = (np.abs(v1) * np.abs(tapsum[sy * 8 + sx])).sum()
+    assert abs(a.sum() - expect) <= 1e-6 * bound

@@ -1,0 +1,119 @@
+"""CPU tests of the oracle itself: before the oracle checks the GPU path, it
+is pinned against outputs of the reference's own CPU gridder (golden
+fixtures made by tests/golden/make_golden.py from grid.cu's gridCPU_pz) and,
+where the reference checkout is present, against that code directly."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import GOLDEN_CASES, load_golden
+
+REF_TAGS = ["64_8_1_double", "64_8_4_double", "64_32_1_double",
+            "128_16_1_double", "256_8_1_double", "64_8_1_double_dbg"]
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_port_matches_golden_bit_exact(name):
+    g = load_golden(name)
+    out = O.grid_pz(g["uv"], g["vals"], g["gcf"], g["N"], g["S"], pols=g["P"],
+                    debug1=g["debug1"])
+    assert np.array_equal(out, g["out"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_multithreaded_port_bit_identical(name):
+    g = load_golden(name)
+    a = O.grid_pz(g["uv"], g["vals"], g["gcf"], g["N"], g["S"], pols=g["P"],
+                  debug1=g["debug1"])
+    b = O.grid_pz(g["uv"], g["vals"], g["gcf"], g["N"], g["S"], pols=g["P"],
+                  debug1=g["debug1"], nthreads=7)
+    assert np.array_equal(a, b)
+
+
+def test_golden_has_clipped_and_offgrid_visibilities():
+    g = load_golden("gauss_n64_s8")
+    uv = g["uv"]
+    assert (uv < 0).any() and (uv >= g["N"]).any()
+    # DEBUG1: every hit count is an integer, and the footprint total is the
+    # number of on-grid taps
+    d = load_golden("debug1_n64_s8")
+    counts = d["out"][0, 0]
+    assert np.array_equal(counts, np.round(counts))
+    S, N = d["S"], d["N"]
+    m = np.floor(d["uv"]).astype(int)
+    taps = 0
+    for mx, my in m:
+        xs = np.arange(mx - S // 2 + 1, mx + S // 2 + 1)
+        ys = np.arange(my - S // 2 + 1, my + S // 2 + 1)
+        taps += ((xs >= 0) & (xs < N)).sum() * ((ys >= 0) & (ys < N)).sum()
+    assert counts.sum() == taps
+
+
+@pytest.mark.parametrize("tag", REF_TAGS)
+def test_port_matches_reference_code(tag):
+    if not O.ref_available(tag):
+        pytest.skip("reference checkout not compiled here (oracle/_ref)")
+    R = O.RefLib(tag)
+    N, S, P = R.img, R.gcf_dim, R.pols
+    rng = np.random.default_rng(hash(tag) % 1000)
+    uv = rng.uniform(-S, N + S, size=(900, 2)).astype(np.float32).astype(np.float64)
+    vals = rng.standard_normal((900 * P, 2))
+    gcf, _ = O.gaussian_gcf(S)
+    assert np.array_equal(R.grid(uv, vals, gcf),
+                          O.grid_pz(uv, vals, gcf, N, S, pols=P, debug1=bool(R.debug1)))
+
+
+def test_reference_nonsense_gcf_and_harness_inputs():
+    if not O.ref_available("64_8_1_double"):
+        pytest.skip("reference checkout not compiled here (oracle/_ref)")
+    R = O.RefLib("64_8_1_double")
+    uv, vals = R.harness_inputs(500)
+    g = R.init_gcf()
+    assert np.array_equal(R.grid(uv, vals, g), O.grid_pz(uv, vals, g, 64, 8))
+
+
+def test_index_step_formulas_agree_on_float_representable():
+    rng = np.random.default_rng(3)
+    uv = rng.uniform(-50, 5000, size=(20000, 2)).astype(np.float32).astype(np.float64)
+    uv[:10] = [[0, 0], [1, 1], [-1, -1], [7.875, 7.999], [4095.875, 0.125],
+               [-0.125, -7.5], [2.5, 3.5], [100, 200], [1e-3, 1e-3], [-1e-3, 5]]
+    uv[:10] = uv[:10].astype(np.float32).astype(np.float64)
+    a = O.vis2ints(uv)
+    b = O.vis2ints(uv, gpu_formula=True)
+    assert np.array_equal(a, b)
+    m = np.floor(uv).astype(np.int64)
+    s = np.floor(8 * (uv - m)).astype(np.int64)
+    assert np.array_equal(a, (m * 8 + s).astype(np.int32))
+
+
+def test_index_step_follows_cpu_formula_below_integer():
+    # u just below an integer, not float-representable: the CPU gridder's
+    # floorf((float)u) rounds up, so its oversample index is -1 while the
+    # all-double GPU driver formula gives 7 (grid.cu:159 vs grid_gpu.cu:118)
+    u = np.array([[99.99999999, 10.5]])
+    a = O.vis2ints(u)
+    b = O.vis2ints(u, gpu_formula=True)
+    assert a[0, 0] == 99 * 8 - 1
+    assert b[0, 0] == 99 * 8 + 7
+
+
+def test_bookmarks_are_lower_bounds():
+    rng = np.random.default_rng(4)
+    N, T = 256, 32
+    uv = rng.uniform(0, N, size=(5000, 2)).astype(np.float32).astype(np.float64)
+    pk = O.vis2ints(uv)
+    tile = (pk[:, 1] // 8 // T) * (N // T) + pk[:, 0] // 8 // T
+    order = np.argsort(tile, kind="stable")
+    bm = O.set_bookmarks(pk[order], T, N // T)
+    expect = np.searchsorted(tile[order], np.arange(N // T * N // T + 1), "left")
+    assert np.array_equal(bm, expect)
+
+
+def test_gaussian_gcf_is_separable_and_peaks_at_centre():
+    tab, g1 = O.gaussian_gcf(16)
+    assert tab.shape == (64, 16, 16)
+    assert np.allclose(tab.imag, 0)
+    # sub-kernel 0: sample distance a - 0 is zero at a' = S/2 - 1
+    assert g1[0].argmax() == 16 // 2 - 1 and g1[0].max() == 1.0
+    t2 = O.gcf_from_1d(g1)
+    assert np.array_equal(tab, t2)
