@@ -192,6 +192,28 @@ int gg_bin(gg_context *ctx, const gg_options *opt, int uv_type, const void *uv,
            int64_t npts, int64_t img_dim, int64_t gcf_dim, int32_t *bookmarks,
            int32_t *order, void *stream);
 
+/* ---- allocation-free moving window -------------------------------------
+ * No counterpart in the reference.  Grids one job like gg_grid_device with
+ * the moving-window method, but every scratch buffer (tile histogram,
+ * bookmarks, sorted visibilities, work queue, counters) comes from a fixed
+ * array compiled into libgg.so instead of an allocation.  It is for callers
+ * that must not allocate device memory while they run: a real-time ingest
+ * that reserves all of its GPU memory at start-up because cudaMalloc can
+ * block on the device or fail mid-observation, or a plugin inside a host
+ * framework that owns the device memory pool.  The caller passes inputs and
+ * outputs (device pointers) as for gg_grid_device.
+ * Limits: npts <= 262144; at most 16384 uv tiles (img_dim <= 4096 at the
+ * default 32-cell tile); one polarisation; complex64 values.  Larger jobs are
+ * rejected with GG_ERR_ARG.  The array (about 9 MiB) stays resident on every
+ * GPU that loads libgg.so until the process exits.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current: make that first call
+ * before any stream capture.  All calls share the array and clear what must
+ * start at zero; calls that overlap on the GPU (other streams or threads)
+ * race on it. */
+int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
+                           void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -28,6 +28,11 @@ static std::atomic<long long> g_launches{0};
 
 void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+int set_error(int code, const char *msg) {
+  g_last_error = msg ? msg : "";
+  return code;
+}
+
 static int fail(int code, const char *fmt, ...) {
   char buf[512];
   va_list ap;

@@ -10,6 +10,8 @@ namespace gg {
 
 // process-wide count of kernel launches made by the library
 void count_launch(int n = 1);
+// records msg as the calling thread's gg_last_error() and returns code
+int set_error(int code, const char *msg);
 
 // One job of a binning pass.  Visibilities of all jobs of a batch live in one
 // global index space: job j owns global indices [vis_base, vis_base+npts) and

@@ -1,0 +1,245 @@
+// gg_grid_device_noalloc: the moving-window gridding path with every scratch
+// buffer carved from one file-scope __device__ array instead of a context
+// workspace, so that a call allocates nothing.
+//
+// Who needs it: callers that must not allocate device memory once they are
+// running -- e.g. a real-time visibility ingest that reserves all of its GPU
+// memory at start-up and forbids cudaMalloc in the data path (cudaMalloc can
+// block on the device and can fail mid-observation), or a plugin loaded into
+// a host framework that owns the device memory pool and does not let plugins
+// allocate behind its back.  They pass inputs and outputs; the library
+// supplies a fixed scratch area.
+//
+// Limits: at most kNoAllocMaxVis visibilities, img_dim up to 4096 with the
+// default 32-cell tile (kNoAllocMaxTiles uv tiles), one polarisation,
+// complex64 values.  The array (about 9 MiB) is held by every GPU that loads
+// this library until the process exits.
+//
+// Set-up: the first call on a device looks up the device address of the
+// array with cudaGetSymbolAddress while that device is current, and caches
+// it; make that first call before any stream capture.  All calls share the
+// array, which keeps whatever the last call left in it: every call clears
+// what must start at zero (histogram, counters, flags, the output grid), and
+// calls that overlap on the GPU (different streams, or different host
+// threads) race on the scratch and corrupt each other's results.
+#include <cstring>
+#include <mutex>
+
+#include "gg_internal.h"
+
+namespace gg {
+namespace {
+
+constexpr int64_t kNoAllocMaxVis = 1 << 18;
+constexpr int kNoAllocMaxTiles = 16384;
+constexpr int kNoAllocChunk = 2048;
+constexpr int kNoAllocMaxDevices = 64;
+constexpr int64_t kClassCap = kNoAllocMaxTiles + kNoAllocMaxVis / kNoAllocChunk + 2;
+
+constexpr size_t al(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// scratch layout (byte offsets)
+constexpr size_t kOffJobs = 0;
+constexpr size_t kOffBin = kOffJobs + al(sizeof(JobDesc));
+constexpr size_t kOffVisBase = kOffBin + al(sizeof(BinJob));
+constexpr size_t kOffTileBase = kOffVisBase + al(2 * sizeof(int64_t));
+constexpr size_t kOffClass = kOffTileBase + al(2 * sizeof(int));
+constexpr size_t kOffFlags = kOffClass + al(sizeof(int));
+constexpr size_t kOffPacked = kOffFlags + al(16 * sizeof(int));
+constexpr size_t kOffKey = kOffPacked + al(sizeof(int2) * (kNoAllocMaxVis + 1));
+constexpr size_t kOffBm = kOffKey + al(sizeof(int) * (kNoAllocMaxVis + 1));
+constexpr size_t kOffCursor = kOffBm + al(sizeof(int) * (kNoAllocMaxTiles + 8));
+constexpr size_t kOffScan = kOffCursor + al(sizeof(int) * (kNoAllocMaxTiles + 8));
+// scan scratch for up to max(tiles, vis)+1 entries: 2048-entry blocks
+constexpr size_t kScanInts = (kNoAllocMaxVis + 1) / 2048 + 64;
+constexpr size_t kOffKept = kOffScan + al(sizeof(int) * kScanInts);
+constexpr size_t kOffSidx = kOffKept + al(sizeof(int) * (kNoAllocMaxVis + 8));
+constexpr size_t kOffSvals = kOffSidx + al(sizeof(int2) * (kNoAllocMaxVis + 8));
+constexpr size_t kOffItems = kOffSvals + al(sizeof(float2) * (kNoAllocMaxVis + 8) + 64);
+constexpr size_t kScratchBytes = kOffItems + al(sizeof(WorkItem) * 4 * kClassCap);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+std::mutex g_setup_mu;
+void *g_scratch_ptr[kNoAllocMaxDevices];
+
+int setup_scratch(char **out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return GG_ERR_CUDA;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return GG_ERR_ARG;
+  std::lock_guard<std::mutex> lk(g_setup_mu);
+  if (!g_scratch_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return GG_ERR_CUDA;
+    g_scratch_ptr[dev] = p;
+  }
+  *out = (char *)g_scratch_ptr[dev];
+  return GG_OK;
+}
+
+int ilog2i(int v) {
+  int l = 0;
+  while ((1 << l) < v) ++l;
+  return l;
+}
+
+int noalloc_fail(int code, const char *m) { return set_error(code, m); }
+
+}  // namespace
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
+                                      void *stream) {
+  if (!opt || !job) return noalloc_fail(GG_ERR_ARG, "noalloc: null argument");
+  const int mode = opt->mode == GG_MODE_AUTO ? GG_MODE_WINDOW : opt->mode;
+  if (mode != GG_MODE_WINDOW)
+    return noalloc_fail(GG_ERR_ARG, "noalloc: only the moving-window method");
+  if (opt->polarizations != 1)
+    return noalloc_fail(GG_ERR_ARG, "noalloc: one polarisation only");
+  if (opt->gcf_kind != GG_GCF_TABLE && opt->gcf_kind != GG_GCF_GAUSSIAN)
+    return noalloc_fail(GG_ERR_ARG, "noalloc: GCF must be TABLE or GAUSSIAN");
+  const int G = opt->oversample, T = opt->tile;
+  if (G < 1 || G > 64 || (G & (G - 1)) || T < 16 || T > 256 || (T & (T - 1)))
+    return noalloc_fail(GG_ERR_ARG, "noalloc: oversample / tile not a power of two in range");
+  if (job->vals_type != GG_C64)
+    return noalloc_fail(GG_ERR_ARG, "noalloc: complex64 values only");
+  if ((job->uv_type != GG_C64 && job->uv_type != GG_C128) ||
+      (job->out_type != GG_C64 && job->out_type != GG_C128))
+    return noalloc_fail(GG_ERR_ARG, "noalloc: bad uv_type / out_type");
+  const int64_t S = job->gcf_dim, N = job->img_dim, n = job->npts;
+  if (S != 4 && S != 8 && S != 16 && S != 32)
+    return noalloc_fail(GG_ERR_ARG, "noalloc: gcf_dim not in {4,8,16,32}");
+  if (n < 0 || n > kNoAllocMaxVis)
+    return noalloc_fail(GG_ERR_ARG,
+                        "noalloc: npts exceeds the fixed scratch (max 262144 visibilities)");
+  const int64_t ntx = (N + T - 1) / T;
+  if (N < 1 || ntx * ntx > kNoAllocMaxTiles)
+    return noalloc_fail(GG_ERR_ARG,
+                        "noalloc: img_dim exceeds the fixed scratch (max 16384 uv tiles, "
+                        "i.e. 4096 at tile 32)");
+  if (!job->out || (n > 0 && (!job->uv || !job->vals)) ||
+      (opt->gcf_kind == GG_GCF_TABLE && !job->gcf))
+    return noalloc_fail(GG_ERR_ARG, "noalloc: null buffer");
+
+  char *ws = nullptr;
+  int st = setup_scratch(&ws);
+  if (st) return noalloc_fail(st, "noalloc: cudaGetSymbolAddress failed");
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return noalloc_fail(GG_ERR_CUDA, "noalloc: device");
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return noalloc_fail(GG_ERR_CUDA, "noalloc: device attribute");
+
+  // device tables, built on the host and copied into the scratch
+  JobDesc D;
+  std::memset(&D, 0, sizeof D);
+  D.out = job->out;
+  D.uv = job->uv;
+  D.gcf = job->gcf;
+  D.idx = (const int2 *)(ws + kOffSidx);
+  D.vals = ws + kOffSvals;
+  D.bookmarks = (const int *)(ws + kOffBm);
+  D.npts = n;
+  D.vstride = kNoAllocMaxVis + 8;
+  D.N = (int)N;
+  D.S = (int)S;
+  D.G = G;
+  D.log2G = ilog2i(G);
+  D.P = 1;
+  D.T = T;
+  D.log2T = ilog2i(T);
+  D.ntx = (int)ntx;
+  D.planar = opt->layout == GG_LAYOUT_PLANAR || opt->layout == GG_LAYOUT_REFERENCE;
+  D.out_f64 = job->out_type == GG_C128;
+  D.uv_f64 = job->uv_type == GG_C128;
+  const double sg = job->gcf_sigma > 0 ? job->gcf_sigma
+                                       : (opt->gcf_sigma > 0 ? opt->gcf_sigma : S / 4.0);
+  D.sigma = (float)sg;
+  BinJob B;
+  std::memset(&B, 0, sizeof B);
+  B.uv = job->uv;
+  B.vals = job->vals;
+  B.vis_base = 0;
+  B.npts = n;
+  B.tile_base = 0;
+  B.ntiles = (int)(ntx * ntx);
+  B.N = (int)N;
+  B.S = (int)S;
+  B.G = G;
+  B.log2G = D.log2G;
+  B.log2T = D.log2T;
+  B.ntx = (int)ntx;
+  B.P = 1;
+  B.uv_f64 = D.uv_f64;
+  const int64_t vis_base[2] = {0, n};
+  const int tile_base[2] = {0, (int)(ntx * ntx)};
+  const int cls = 0;
+#define GG_NA(call)                                                        \
+  do {                                                                     \
+    if ((call) != cudaSuccess) return noalloc_fail(GG_ERR_CUDA, "noalloc: " #call); \
+  } while (0)
+  GG_NA(cudaMemcpyAsync(ws + kOffJobs, &D, sizeof D, cudaMemcpyHostToDevice, s));
+  GG_NA(cudaMemcpyAsync(ws + kOffBin, &B, sizeof B, cudaMemcpyHostToDevice, s));
+  GG_NA(cudaMemcpyAsync(ws + kOffVisBase, vis_base, sizeof vis_base, cudaMemcpyHostToDevice, s));
+  GG_NA(cudaMemcpyAsync(ws + kOffTileBase, tile_base, sizeof tile_base,
+                        cudaMemcpyHostToDevice, s));
+  GG_NA(cudaMemcpyAsync(ws + kOffClass, &cls, sizeof cls, cudaMemcpyHostToDevice, s));
+  // pageable-source copies above complete before returning to the host, so
+  // the stack tables may go out of scope
+  int *flags = (int *)(ws + kOffFlags);
+  GG_NA(cudaMemsetAsync(flags, 0, 16 * sizeof(int), s));
+  const size_t out_bytes = (size_t)(D.out_f64 ? 16 : 8) * N * N;
+  GG_NA(cudaMemsetAsync(job->out, 0, out_bytes, s));
+
+  BinBuffers b{};
+  b.jobs = (const BinJob *)(ws + kOffBin);
+  b.vis_base = (const int64_t *)(ws + kOffVisBase);
+  b.tile_base = (const int *)(ws + kOffTileBase);
+  b.njobs = 1;
+  b.total_vis = n;
+  b.total_tiles = (int)(ntx * ntx);
+  b.vals_bytes = 8;
+  b.P = 1;
+  b.packed = (int2 *)(ws + kOffPacked);
+  b.key = (int *)(ws + kOffKey);
+  b.bookmarks = (int *)(ws + kOffBm);
+  b.cursor = (int *)(ws + kOffCursor);
+  b.scan_tmp = (int *)(ws + kOffScan);
+  b.sorted_idx = (int2 *)(ws + kOffSidx);
+  b.sorted_vals = ws + kOffSvals;
+  b.vstride = kNoAllocMaxVis + 8;
+  b.order = nullptr;
+  b.flags = flags;
+  b.input_sorted = opt->input_sorted ? 1 : 0;
+  b.kept_pos = b.input_sorted ? (int *)(ws + kOffKept) : nullptr;
+  GG_NA(run_binning(b, s));
+
+  WorkItem *items = (WorkItem *)(ws + kOffItems);
+  GG_NA(launch_make_items(b.bookmarks, b.tile_base, (const int *)(ws + kOffClass), 1,
+                          b.total_tiles, kNoAllocChunk, items, kClassCap, flags + 8, s));
+  GridLaunch g{};
+  g.jobs = (const JobDesc *)(ws + kOffJobs);
+  g.njobs = 1;
+  g.S = (int)S;
+  g.accum = opt->accum;
+  g.vals_f64 = 0;
+  g.gauss = opt->gcf_kind == GG_GCF_GAUSSIAN;
+  g.sigma = (float)sg;
+  g.G = G;
+  g.tile = T;
+  g.P = 1;
+  g.flags = flags;
+  g.sm_count = sms;
+  g.items = items;
+  g.nitems = flags + 8;
+  g.item_next = flags + 12;
+  g.max_items = kClassCap;
+  GG_NA(launch_window(g, s));
+#undef GG_NA
+  return GG_OK;
+}
