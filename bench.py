@@ -42,7 +42,7 @@ WORKLOADS = {
     # gather / moving-window workload
     "tracks4096": dict(
         N=4096, S=8, npts=1 << 22, gen="tracks", vals="c64", out="c64",
-        mode="auto", accum="comp", input_sorted=True,
+        mode="auto", accum="comp", presort=True, input_sorted=False,
         desc=("4096^2 complex64 grid; 2^22 visibilities on uv tracks (64 "
               "antennas in a 2 km disk, 2016 baselines x 2080 hour angles over "
               "+-4 h at dec -30 deg, 90% fill, +1024 to 2^22); complex64 N(0,1) "
@@ -83,7 +83,9 @@ def make_inputs(w, seed):
         uv, vals = synth.disk(n, N, seed=seed, outlier_frac=0.01, vals_dtype=vdt)
     else:
         uv, vals = synth.uniform(n, S, N - S, seed=seed, vals_dtype=vdt)
-    if w.get("input_sorted"):
+    if w.get("presort"):
+        # the data format of the workload: grouped into 32x32 uv tiles; the
+        # gridder still bins on the device at its own tile size
         perm = synth.tile_sort(uv, N, 32)
         uv, vals = np.ascontiguousarray(uv[perm]), np.ascontiguousarray(vals[perm])
     g1 = synth.gaussian_gcf_1d(S)

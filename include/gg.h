@@ -77,16 +77,20 @@ typedef struct gg_options {
   int32_t gcf_kind;      /* GG_GCF_*                                         */
   int32_t oversample;    /* GCF_GRID: power of two, 1..64 (default 8)        */
   int32_t polarizations; /* POLARIZATIONS: 1..8 (default 1)                  */
-  int32_t tile;          /* uv tile side in cells for binning (default 32)   */
+  int32_t tile;          /* uv tile side in cells for binning; 0 = chosen by
+                            method and support (default)                  */
   int32_t input_sorted;  /* 1: caller guarantees visibilities are grouped by
-                            uv tile in ascending tile id (checked)            */
+                            uv tile (of `tile` cells, 32 when tile is 0) in
+                            ascending tile id (checked)                      */
   double gcf_sigma;      /* GG_GCF_GAUSSIAN: sigma in cells; 0 -> S/4        */
   int32_t window_chunk;  /* max visibilities per work item (0 -> default)    */
-  int32_t reserved[7];
+  int32_t group_warps;   /* moving window: warps sharing one sub-grid
+                            (1, 2, 4 or 8; 0 -> chosen by support)           */
+  int32_t reserved[6];
 } gg_options;
 
 /* Defaults = the reference built with no Makefile switches: SCATTER,
- * REFERENCE layout, PLAIN, TABLE, G=8, P=1; tile 32. */
+ * REFERENCE layout, PLAIN, TABLE, G=8, P=1; automatic tile. */
 int gg_default_options(gg_options *opt);
 
 /* Process-wide options used by the drop-in gridGPU entry points below, the

@@ -126,7 +126,7 @@ static gg_options default_opts() {
   o.gcf_kind = GG_GCF_TABLE;
   o.oversample = 8;
   o.polarizations = 1;
-  o.tile = 32;
+  o.tile = 0;
   o.input_sorted = 0;
   o.gcf_sigma = 0.0;
   o.window_chunk = 0;
@@ -152,10 +152,13 @@ static int check_options(const gg_options *o) {
   if (o->polarizations < 1 || o->polarizations > kMaxPols)
     return fail(GG_ERR_ARG, "options: polarizations %d outside 1..%d",
                 o->polarizations, kMaxPols);
-  if (!is_pow2(o->tile) || o->tile < 16 || o->tile > 256)
-    return fail(GG_ERR_ARG, "options: tile %d must be a power of two in 16..256",
+  if (o->tile != 0 && (!is_pow2(o->tile) || o->tile < 16 || o->tile > 256))
+    return fail(GG_ERR_ARG, "options: tile %d must be 0 or a power of two in 16..256",
                 o->tile);
   if (o->window_chunk < 0) return fail(GG_ERR_ARG, "options: window_chunk < 0");
+  if (o->group_warps != 0 && o->group_warps != 1 && o->group_warps != 2 &&
+      o->group_warps != 4 && o->group_warps != 8)
+    return fail(GG_ERR_ARG, "options: group_warps %d not in {0,1,2,4,8}", o->group_warps);
   return GG_OK;
 }
 
@@ -169,7 +172,7 @@ struct Plan {
   int vals_f64 = 0;
   int gauss = 0;
   float sigma = 0.f;
-  int G = 8, P = 1, T = 32, chunk = 2048;
+  int G = 8, P = 1, T = 32, chunk = 2048, group_warps = 0;
   int njobs = 0;
   int64_t total_vis = 0;
   int total_tiles = 0;
@@ -265,8 +268,18 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
   pl = Plan();
   pl.G = opt->oversample;
   pl.P = opt->polarizations;
-  pl.T = opt->tile;
+  {
+    // automatic tile: the moving window keeps one (T+S-1)^2 sub-grid per warp
+    // group, so small supports use 16-cell tiles; gather needs 32
+    int64_t maxS = 0;
+    for (int j = 0; j < njobs; ++j) maxS = std::max<int64_t>(maxS, jobs[j].gcf_dim);
+    const int m0 = resolve_mode(opt, (int)maxS);
+    // (input declared tile-sorted: the caller's tiles are the default 32)
+    pl.T = opt->tile > 0 ? opt->tile
+                         : (m0 == GG_MODE_WINDOW && maxS <= 16 && !opt->input_sorted ? 16 : 32);
+  }
   pl.chunk = opt->window_chunk > 0 ? opt->window_chunk : 2048;
+  pl.group_warps = opt->group_warps;
   pl.input_sorted = opt->input_sorted ? 1 : 0;
   pl.gauss = opt->gcf_kind == GG_GCF_GAUSSIAN;
   pl.accum = opt->accum;
@@ -331,6 +344,17 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
   if (vis >= (1ll << 31) - 1024) return fail(GG_ERR_ARG, "batch has >= 2^31 visibilities");
   if (tiles >= (1ll << 30)) return fail(GG_ERR_ARG, "batch has too many uv tiles");
   pl.mode = mode;
+  if (mode == GG_MODE_WINDOW) {
+    for (int j = 0; j < njobs; ++j) {
+      const size_t need = window_smem_bytes((int)jobs[j].gcf_dim, opt->accum,
+                                            vt == GG_C128, pl.T, pl.group_warps);
+      if (need > 227 * 1024)
+        return fail(GG_ERR_ARG,
+                    "tile %d with support %lld needs %zu bytes of shared memory "
+                    "(max 232448): use a smaller tile",
+                    pl.T, (long long)jobs[j].gcf_dim, need);
+    }
+  }
   pl.sigma = (float)(sigma > 0 ? sigma : 0.0);
   pl.total_vis = vis;
   pl.total_tiles = (int)tiles;
@@ -543,6 +567,7 @@ static int plan_execute(gg_context *c, const gg_options *opt, Plan &pl,
   g.sigma = pl.sigma;
   g.G = pl.G;
   g.tile = pl.T;
+  g.group_warps = pl.group_warps;
   g.P = pl.P;
   g.flags = flags;
   g.sm_count = c->sm_count;

@@ -26,9 +26,32 @@ namespace gg {
 // same conversions so that main and sub are bit-exact with the CPU gridder
 // for every finite u.  For float-representable u the result also equals the
 // GPU driver's all-double formula (grid_gpu.cu:118-121, 358-363).
+// The step for float coordinates with |u| < 2^23, entirely in FP32:
+// floorf(u) is exact, u - floorf(u) is exact and so is the power-of-two scale,
+// so this equals the double formula below on (double)u.
+__device__ __forceinline__ void index_step_f32(float u, int G, int &m, int &s) {
+  float fl = floorf(u);
+  s = (int)floorf(__fmul_rn((float)G, __fsub_rn(u, fl)));
+  m = (int)fl;
+}
+
 // Returns false when u is not finite or |u| >= 2^24 (no grid is that large;
 // the bound keeps the packed main*G+sub inside int32 for G <= 64).
+// GB300's FP64 pipe is narrow, so a coordinate that is exactly representable
+// as a normal float with |u| < 2^23 -- the convention of the reference
+// harness and of float-precision callers -- is recognised from its bits and
+// takes the exact FP32 form; every other value takes the FP64 expression.
 __device__ __forceinline__ bool index_step(double u, int G, int &m, int &s) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(u);
+  const unsigned hi = (unsigned)(bits >> 32), lo = (unsigned)bits;
+  const unsigned E = (hi >> 20) & 0x7ffu;
+  if ((lo & 0x1fffffffu) == 0u && E >= 897u && E <= 1045u) {
+    // 2^-126 <= |u| < 2^23 and the low 29 mantissa bits are zero
+    const float f = __int_as_float((int)((hi & 0x80000000u) | ((E - 896u) << 23) |
+                                         ((hi & 0x000fffffu) << 3) | (lo >> 29)));
+    index_step_f32(f, G, m, s);
+    return true;
+  }
   if (!(u > -16777216.0 && u < 16777216.0)) return false;
   float uf = __double2float_rn(u);
   double frac = __dmul_rn((double)G, __dsub_rn(u, (double)floorf(uf)));
@@ -37,14 +60,10 @@ __device__ __forceinline__ bool index_step(double u, int G, int &m, int &s) {
   return true;
 }
 
-// The same step for float coordinates, entirely in FP32: floorf(u) is exact,
-// u - floorf(u) is exact for |u| < 2^23 and the power-of-two scale is exact,
-// so this equals index_step((double)u, ...) on those inputs.
+// The same step for float coordinates.
 __device__ __forceinline__ bool index_step(float u, int G, int &m, int &s) {
-  if (!(u > -8.0e6f && u < 8.0e6f)) return false;
-  float fl = floorf(u);
-  s = (int)floorf(__fmul_rn((float)G, __fsub_rn(u, fl)));
-  m = (int)fl;
+  if (!(u > -8388608.0f && u < 8388608.0f)) return false;
+  index_step_f32(u, G, m, s);
   return true;
 }
 

@@ -44,9 +44,9 @@ __global__ void __launch_bounds__(kGatherThreads)
   constexpr int K = kGatherChunk, H = S / 2, TT = kGatherTile;
   extern __shared__ __align__(16) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-  unsigned char *idxbuf[2] = {smem + 16, smem + 16 + Sh::IDX_BUF};
-  unsigned char *valbuf[2] = {smem + 16 + 2 * Sh::IDX_BUF,
-                              smem + 16 + 2 * Sh::IDX_BUF + Sh::VAL_BUF};
+  // double buffers, addressed arithmetically (buffer b at +b*size)
+  unsigned char *const idx0 = smem + 16;
+  unsigned char *const val0 = smem + 16 + 2 * Sh::IDX_BUF;
   int *list = reinterpret_cast<int *>(smem + 16 + 2 * Sh::IDX_BUF + 2 * Sh::VAL_BUF);
   float *g1 = reinterpret_cast<float *>(list + K);
   __shared__ int wcount[kGatherThreads / 32 + 1];
@@ -102,8 +102,8 @@ __global__ void __launch_bounds__(kGatherThreads)
                              (uint32_t)(((v1 + 15) & ~(size_t)15) - (v0 & ~(size_t)15));
             fence_proxy_async();
             mbar_expect_tx(&bar[b], bytes);
-            stage_span(idxbuf[b], reinterpret_cast<const char *>(J.idx), i0, i1, &bar[b]);
-            stage_span(valbuf[b], reinterpret_cast<const char *>(vplane), v0, v1, &bar[b]);
+            stage_span((idx0 + b * Sh::IDX_BUF), reinterpret_cast<const char *>(J.idx), i0, i1, &bar[b]);
+            stage_span((val0 + b * Sh::VAL_BUF), reinterpret_cast<const char *>(vplane), v0, v1, &bar[b]);
           };
           if (tid == 0 && nchunks > 0) {
             issue(0, 0);
@@ -118,8 +118,8 @@ __global__ void __launch_bounds__(kGatherThreads)
             if (s_abort) break;
             const int s0 = s_beg + c * K;
             const int m = min(K, s_end - s0);
-            const int2 *ib = reinterpret_cast<const int2 *>(idxbuf[b] + (((size_t)s0 * 8) & 15));
-            const VT2 *vb = reinterpret_cast<const VT2 *>(valbuf[b] + (((size_t)s0 * sizeof(VT2)) & 15));
+            const int2 *ib = reinterpret_cast<const int2 *>((idx0 + b * Sh::IDX_BUF) + (((size_t)s0 * 8) & 15));
+            const VT2 *vb = reinterpret_cast<const VT2 *>((val0 + b * Sh::VAL_BUF) + (((size_t)s0 * sizeof(VT2)) & 15));
             // compaction: records whose footprint overlaps this tile, in order
             int base = 0;
             for (int r0 = 0; r0 < m; r0 += kGatherThreads) {

@@ -79,6 +79,7 @@ struct GridLaunch {
   float sigma;             // GAUSS: uniform over the launch
   int G;                   // oversampling, uniform over the launch
   int tile;                // uv tile side, uniform over the launch
+  int group_warps;         // moving window: warps per sub-grid (0: by support)
   int P;
   int *flags;
   int sm_count;
@@ -106,6 +107,6 @@ cudaError_t launch_comp_finalize(float *out, const float *lo, int64_t n,
 cudaError_t launch_count_inputs(void *vals, int vals_f64, int64_t npts, int P,
                                 void *gcf, int64_t gcf_elems, cudaStream_t s);
 // smem bytes the window kernel needs (for occupancy sizing)
-size_t window_smem_bytes(int S, int accum, int vals_f64);
+size_t window_smem_bytes(int S, int accum, int vals_f64, int T, int group_warps);
 
 }  // namespace gg

@@ -102,7 +102,7 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
     return noalloc_fail(GG_ERR_ARG, "noalloc: one polarisation only");
   if (opt->gcf_kind != GG_GCF_TABLE && opt->gcf_kind != GG_GCF_GAUSSIAN)
     return noalloc_fail(GG_ERR_ARG, "noalloc: GCF must be TABLE or GAUSSIAN");
-  const int G = opt->oversample, T = opt->tile;
+  const int G = opt->oversample, T = opt->tile > 0 ? opt->tile : 32;
   if (G < 1 || G > 64 || (G & (G - 1)) || T < 16 || T > 256 || (T & (T - 1)))
     return noalloc_fail(GG_ERR_ARG, "noalloc: oversample / tile not a power of two in range");
   if (job->vals_type != GG_C64)

@@ -1,313 +1,521 @@
 // Moving-window gridding (the reference's MOVING_WINDOW method,
 // grid_kernel_window, grid_gpu.cu:504-673), rebuilt for sm_103a.
 //
-// The reference gives each thread a fixed residue (x mod S, y mod S), keeps a
-// register sum while the target cell of consecutive (sorted) visibilities is
-// unchanged and flushes it with a global CAS atomic when the cell changes.
-// Here:
-//  * a persistent CTA pulls work items -- slices of one uv tile's sorted
-//    visibilities -- from a device queue, so dense tiles are split across SMs
-//    and sparse ones are packed together;
-//  * every CTA owns a (T+S-1)^2 shared-memory sub-grid covering its tile plus
-//    the footprint halo; register sums are flushed there (FP32 compensated
-//    hi/lo when requested) and the sub-grid is flushed to HBM ONCE per item,
-//    with native vector reductions and only for cells that were touched;
-//  * residue threads: S*S of them own distinct residues, so within one
-//    visibility group no two threads ever write the same cell; with S*S <
-//    256, several groups split each staged chunk and flush with shared
-//    atomics instead;
-//  * visibility records (packed indices + values) are staged in shared memory
-//    by 1-D TMA bulk copies, double-buffered on two mbarriers.
-// Items too sparse to pay for zeroing and flushing the sub-grid flush each
-// register sum straight to HBM instead.
+// The reference gives each thread a fixed residue (x mod S, y mod S) of the
+// support, keeps a register sum while the target cell of consecutive (sorted)
+// visibilities is unchanged and flushes it with a global CAS atomic when the
+// cell changes.  The property that makes this work is kept and pushed further:
+// a cell (x, y) is only ever reached through residue (x mod S, y mod S), so
+// the thread that owns that residue is the only one that ever touches it.
+//
+//  * Work is split into independent groups of W warps.  Each group owns a
+//    private (T+S-1)^2 shared-memory sub-grid covering one uv tile plus the
+//    footprint halo, its own double-buffered TMA staging area and mbarriers,
+//    and pulls work items (slices of one tile's sorted visibilities) from the
+//    device queue on its own: groups never wait for each other.
+//  * Inside a group every thread owns Q = S*S/(32 W) residues of one column.
+//    For each residue it keeps a register sum while the target cell stays the
+//    same and, when it changes, adds the sum into the sub-grid.  Ownership
+//    makes that read-modify-write exclusive: no atomics, and no
+//    synchronisation between visibilities.
+//  * FP32 sums are compensated: a (hi, lo) pair per component updated with
+//    Knuth's TwoSum on the packed (re, im) pair (f32x2 instructions), in
+//    registers and again when a register sum is added into the sub-grid.
+//  * Visibility records (packed indices + values) stream through shared
+//    memory by 1-D TMA bulk copies, double-buffered, as one continuous stream
+//    across work items (the next item is claimed early and its first chunk
+//    prefetched while the current one is gridded).
+//  * Once per item the sub-grid is flushed to HBM with native vector
+//    reductions (touched cells only) and zeroed as it is read.  Items too
+//    sparse to pay for that flush send each register sum straight to HBM.
 #include "gg_kernels.cuh"
 
 namespace gg {
 
-constexpr int kWinChunk = 512;
+// ---- packed FP32x2 helpers (PTX f32x2, sm_100+) ------------------------------
+typedef unsigned long long u64;
+__device__ __forceinline__ u64 pk2(float a, float b) {
+  u64 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float2 upk2(u64 r) {
+  float2 f;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(f.x), "=f"(f.y) : "l"(r));
+  return f;
+}
+__device__ __forceinline__ u64 add2(u64 a, u64 b) {
+  u64 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
+  u64 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
+  u64 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
+  u64 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+// (s, e) = TwoSum(a, b) on both lanes: s = fl(a+b), a + b = s + e exactly
+__device__ __forceinline__ u64 two_sum2(u64 a, u64 b, u64 &e) {
+  const u64 s = add2(a, b);
+  const u64 bb = sub2(s, a);
+  e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+  return s;
+}
 
-template <class ACC> struct Cell;
-template <> struct Cell<AccF32> { float re, im; };
-template <> struct Cell<AccComp> { float hr, hi, lr, li; };
-template <> struct Cell<AccF64> { double re, im; };
-
-__device__ __forceinline__ void cell_add(Cell<AccF32> *c, const AccF32 &a,
-                                         bool exclusive) {
-  if (exclusive) {
-    c->re = __fadd_rn(c->re, a.re);
-    c->im = __fadd_rn(c->im, a.im);
-  } else {
-    atomicAdd(&c->re, a.re);
-    atomicAdd(&c->im, a.im);
+// ---- per-thread running sums and sub-grid cells -------------------------------
+// MODE 0: plain FP32      sum u64 (re, im)          cell float2
+// MODE 1: compensated     sums u64 hi, lo           cell float4 {hi, lo}
+// MODE 2: FP64            sums double re, im        cell double2
+template <int MODE> struct WinAcc;
+template <> struct WinAcc<0> {
+  using VT = float;
+  using CellT = float2;
+  u64 s;
+  __device__ __forceinline__ void zero() { s = 0ull; }
+  __device__ __forceinline__ void add(u64 t) { s = add2(s, t); }
+  __device__ __forceinline__ void into(CellT *c) const {
+    const float2 o = *c;
+    *c = upk2(add2(pk2(o.x, o.y), s));
   }
-}
-__device__ __forceinline__ void cell_add(Cell<AccComp> *c, const AccComp &a,
-                                         bool exclusive) {
-  float s, e;
-  if (exclusive) {
-    two_sum(c->hr, a.hr, s, e);
-    c->hr = s;
-    c->lr = __fadd_rn(c->lr, __fadd_rn(e, a.lr));
-    two_sum(c->hi, a.hi_, s, e);
-    c->hi = s;
-    c->li = __fadd_rn(c->li, __fadd_rn(e, a.li));
-  } else {
-    // the shared-memory atomic returns the old value; two_sum recovers the
-    // exact rounding error of the addition the hardware just performed
-    float old = atomicAdd(&c->hr, a.hr);
-    two_sum(old, a.hr, s, e);
-    atomicAdd(&c->lr, __fadd_rn(e, a.lr));
-    old = atomicAdd(&c->hi, a.hi_);
-    two_sum(old, a.hi_, s, e);
-    atomicAdd(&c->li, __fadd_rn(e, a.li));
+  __device__ __forceinline__ void out(const JobDesc &J, size_t cell, int p, int P) const {
+    const float2 v = upk2(s);
+    out_red(J, cell, p, P, (double)v.x, (double)v.y);
   }
-}
-__device__ __forceinline__ void cell_add(Cell<AccF64> *c, const AccF64 &a,
-                                         bool exclusive) {
-  if (exclusive) {
-    c->re = __dadd_rn(c->re, a.re);
-    c->im = __dadd_rn(c->im, a.im);
-  } else {
-    atomicAdd(&c->re, a.re);
-    atomicAdd(&c->im, a.im);
+};
+template <> struct WinAcc<1> {
+  using VT = float;
+  using CellT = float4;
+  u64 hi, lo;
+  __device__ __forceinline__ void zero() { hi = lo = 0ull; }
+  __device__ __forceinline__ void add(u64 t) {
+    u64 e;
+    hi = two_sum2(hi, t, e);
+    lo = add2(lo, e);
   }
-}
-
-__device__ __forceinline__ void cell_load(const Cell<AccF32> &c, AccF32 &a) {
-  a.re = c.re; a.im = c.im;
-}
-__device__ __forceinline__ void cell_load(const Cell<AccComp> &c, AccComp &a) {
-  a.hr = c.hr; a.hi_ = c.hi; a.lr = c.lr; a.li = c.li;
-}
-__device__ __forceinline__ void cell_load(const Cell<AccF64> &c, AccF64 &a) {
-  a.re = c.re; a.im = c.im;
-}
-
-template <int S, class ACC>
-struct WinShape {
-  using VT = typename ACC::VT;
-  using VT2 = typename vec2_of<VT>::type;
-  static constexpr int NRES = S * S;
-  static constexpr int NT = NRES > 256 ? NRES : 256;
-  static constexpr int V = NT / NRES;
-  static constexpr int IDX_BUF = kWinChunk * 8 + 16;
-  static constexpr int VAL_BUF = kWinChunk * (int)sizeof(VT2) + 16;
-  // bytes: 2 mbarriers (pad 16) + 2 idx buffers + 2 value buffers + 1-D GCF
-  // factors (64 x S floats max) + the sub-grid
-  static size_t smem(int T) {
-    int R = T + S - 1;
-    return 16 + 2 * IDX_BUF + 2 * VAL_BUF + 64 * S * 4 +
-           (size_t)R * R * sizeof(Cell<ACC>);
+  __device__ __forceinline__ void into(CellT *c) const {
+    const float4 o = *c;
+    u64 e;
+    const u64 h = two_sum2(pk2(o.x, o.y), hi, e);
+    const float2 hf = upk2(h), lf = upk2(add2(pk2(o.z, o.w), add2(e, lo)));
+    *c = make_float4(hf.x, hf.y, lf.x, lf.y);
+  }
+  __device__ __forceinline__ void out(const JobDesc &J, size_t cell, int p, int P) const {
+    const float2 h = upk2(hi), l = upk2(lo);
+    if (J.out_f64)
+      out_red(J, cell, p, P, (double)h.x + (double)l.x, (double)h.y + (double)l.y);
+    else
+      out_red(J, cell, p, P, (double)__fadd_rn(h.x, l.x), (double)__fadd_rn(h.y, l.y));
+  }
+};
+template <> struct WinAcc<2> {
+  using VT = double;
+  using CellT = double2;
+  double re, im;
+  __device__ __forceinline__ void zero() { re = im = 0.0; }
+  __device__ __forceinline__ void add(double tr, double ti) {
+    re = __dadd_rn(re, tr);
+    im = __dadd_rn(im, ti);
+  }
+  __device__ __forceinline__ void into(CellT *c) const {
+    const double2 o = *c;
+    *c = make_double2(__dadd_rn(o.x, re), __dadd_rn(o.y, im));
+  }
+  __device__ __forceinline__ void out(const JobDesc &J, size_t cell, int p, int P) const {
+    out_red(J, cell, p, P, re, im);
   }
 };
 
-template <int S, class ACC, bool GAUSS>
-__global__ void __launch_bounds__(WinShape<S, ACC>::NT)
+__device__ __forceinline__ bool cell_nonzero(const float2 &c) { return c.x != 0.f || c.y != 0.f; }
+__device__ __forceinline__ bool cell_nonzero(const float4 &c) {
+  return c.x != 0.f || c.y != 0.f || c.z != 0.f || c.w != 0.f;
+}
+__device__ __forceinline__ bool cell_nonzero(const double2 &c) { return c.x != 0.0 || c.y != 0.0; }
+
+// flush of a finished sub-grid cell into the output grid (reduction)
+__device__ __forceinline__ void out_cell(const JobDesc &J, size_t cell, int p,
+                                         int P, const float2 &c) {
+  out_red(J, cell, p, P, (double)c.x, (double)c.y);
+}
+__device__ __forceinline__ void out_cell(const JobDesc &J, size_t cell, int p,
+                                         int P, const float4 &c) {
+  // complex128 grid: hi+lo exactly; complex64 grid: hi+lo rounded once
+  if (J.out_f64)
+    out_red(J, cell, p, P, (double)c.x + (double)c.z, (double)c.y + (double)c.w);
+  else
+    out_red(J, cell, p, P, (double)__fadd_rn(c.x, c.z), (double)__fadd_rn(c.y, c.w));
+}
+__device__ __forceinline__ void out_cell(const JobDesc &J, size_t cell, int p,
+                                         int P, const double2 &c) {
+  out_red(J, cell, p, P, c.x, c.y);
+}
+
+// ---- configuration ----------------------------------------------------------------
+constexpr int kWinThreads = 256;
+
+// warps per sub-grid group chosen when the caller leaves it open
+// (measured on the 4096^2 track workload: S=8 with 2 warps per group beats 1)
+__host__ __device__ constexpr int win_default_warps(int S) {
+  return S >= 32 ? 8 : (S >= 8 ? 2 : 1);
+}
+
+template <int S, int W> struct WinCfg {
+  static constexpr int NGT = 32 * W;                         // threads per group
+  static constexpr int Q = (S * S + NGT - 1) / NGT;          // residues per thread
+  static constexpr int K = S >= 32 ? 512 : (S >= 16 ? 256 : 128);  // records per chunk
+  static constexpr int GROUPS = kWinThreads / NGT;
+};
+
+template <int S, int W, int MODE>
+struct WinLayout {
+  using Cfg = WinCfg<S, W>;
+  using VT2 = typename vec2_of<typename WinAcc<MODE>::VT>::type;
+  using CellT = typename WinAcc<MODE>::CellT;
+  static constexpr int IDX_BUF = Cfg::K * 8 + 16;
+  static constexpr int VAL_BUF = Cfg::K * (int)sizeof(VT2) + 16;
+  static constexpr int G1_BYTES = 64 * S * 4;
+  // per group: 2 mbarriers (16 B), 2 index buffers, 2 value buffers, sub-grid
+  __host__ __device__ static size_t group_bytes(int T) {
+    const size_t R = (size_t)T + S - 1;
+    return (16 + 2 * IDX_BUF + 2 * VAL_BUF + R * R * sizeof(CellT) + 15) & ~(size_t)15;
+  }
+  __host__ __device__ static size_t cta_bytes(int T) {
+    return G1_BYTES + Cfg::GROUPS * group_bytes(T);
+  }
+};
+
+__device__ __forceinline__ void group_sync(int gid, int nthreads) {
+  if (nthreads == 32) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + gid), "r"(nthreads) : "memory");
+  }
+}
+
+template <int S, int W, int MODE, bool GAUSS>
+__global__ void __launch_bounds__(kWinThreads)
     window_kernel(KParams kp) {
-  using Sh = WinShape<S, ACC>;
-  using VT = typename ACC::VT;
-  using VT2 = typename Sh::VT2;
-  using CellT = Cell<ACC>;
-  constexpr int NRES = Sh::NRES, NT = Sh::NT, V = Sh::V, K = kWinChunk;
+  using Cfg = WinCfg<S, W>;
+  using L = WinLayout<S, W, MODE>;
+  using ACC = WinAcc<MODE>;
+  using VT2 = typename L::VT2;
+  using CellT = typename L::CellT;
+  constexpr int NGT = Cfg::NGT, Q = Cfg::Q, K = Cfg::K, GROUPS = Cfg::GROUPS;
   constexpr int H = S / 2;
 
   extern __shared__ __align__(16) unsigned char smem[];
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-  unsigned char *idxbuf[2] = {smem + 16, smem + 16 + Sh::IDX_BUF};
-  unsigned char *valbuf[2] = {smem + 16 + 2 * Sh::IDX_BUF,
-                              smem + 16 + 2 * Sh::IDX_BUF + Sh::VAL_BUF};
-  float *g1 = reinterpret_cast<float *>(smem + 16 + 2 * Sh::IDX_BUF + 2 * Sh::VAL_BUF);
-  CellT *region = reinterpret_cast<CellT *>(
-      smem + 16 + 2 * Sh::IDX_BUF + 2 * Sh::VAL_BUF + 64 * S * 4);
-  __shared__ int s_item;
-  __shared__ int s_abort;
-
+  float *g1 = reinterpret_cast<float *>(smem);
   const int tid = threadIdx.x;
-  const int res = tid % NRES, grp = tid / NRES;
-  const int rx = res % S, ry = res / S;
+  const int gid = tid / NGT, gt = tid % NGT;
   const int P = kp.P, T = kp.T, R = T + S - 1;
+  const size_t gbytes = L::group_bytes(T);
+  unsigned char *gbase_p = smem + L::G1_BYTES + gid * gbytes;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(gbase_p);
+  unsigned char *const idx0 = gbase_p + 16;
+  unsigned char *const val0 = gbase_p + 16 + 2 * L::IDX_BUF;
+  CellT *region = reinterpret_cast<CellT *>(gbase_p + 16 + 2 * L::IDX_BUF + 2 * L::VAL_BUF);
+  __shared__ int s_item[GROUPS], s_next[GROUPS], s_abort[GROUPS];
 
-  if (tid == 0) {
+  // residues of this thread: r = gt + k*NGT -> column rx (the same for every
+  // k, NGT being a multiple of S), rows ry[k]
+  const int rx = gt % S;
+  int ry[Q];
+  bool rv[Q];
+#pragma unroll
+  for (int k = 0; k < Q; ++k) {
+    const int r = gt + k * NGT;
+    rv[k] = r < S * S;
+    ry[k] = r / S;
+  }
+  const int nitems = *kp.nitems;
+  const bool leader = gt == 0;
+
+  if (leader) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
-    s_abort = 0;
+    s_abort[gid] = 0;
+    const int a = atomicAdd(kp.item_next, 1);
+    s_item[gid] = a;
+    s_next[gid] = a < nitems ? atomicAdd(kp.item_next, 1) : nitems;
   }
+  if constexpr (GAUSS) gauss_fill(g1, S, kp.G, kp.sigma, tid, kWinThreads);
+  for (int i = gt; i < R * R; i += NGT) region[i] = CellT{};
   __syncthreads();
-  uint32_t uses0 = 0, uses1 = 0;  // completed phases of each buffer barrier
-  if constexpr (GAUSS) gauss_fill(g1, S, kp.G, kp.sigma, tid, NT);
-  const int nitems = *kp.nitems;
 
-  for (;;) {
-    if (tid == 0) s_item = atomicAdd(kp.item_next, 1);
-    __syncthreads();
-    const int it = s_item;
-    if (it >= nitems || s_abort) break;
-    const WorkItem w = kp.items[it];
+  // Chunk stream of this group: chunk g lives in buffer g&1, whose (g>>1)-th
+  // use completes barrier phase (g>>1)&1.  The leader keeps two in flight,
+  // looking one (item, plane) ahead.
+  int gfirst = 0;  // stream number of the current (item, plane)'s first chunk
+  int issued = 0, waited = 0;
+  int item = s_item[gid], next = s_next[gid];
+
+  auto issue = [&](int g, int it, int c, int p) {
+    const WorkItem wi = kp.items[it];
+    const int s0 = wi.start + c * K;
+    const int e0 = min(wi.end, s0 + K);
+    const JobDesc &J = kp.jobs[wi.job];
+    const VT2 *vplane = reinterpret_cast<const VT2 *>(J.vals) + (size_t)p * J.vstride;
+    const size_t i0 = (size_t)s0 * 8, i1 = (size_t)e0 * 8;
+    const size_t v0 = (size_t)s0 * sizeof(VT2), v1 = (size_t)e0 * sizeof(VT2);
+    const uint32_t bytes = (uint32_t)(((i1 + 15) & ~(size_t)15) - (i0 & ~(size_t)15)) +
+                           (uint32_t)(((v1 + 15) & ~(size_t)15) - (v0 & ~(size_t)15));
+    const int b = g & 1;
+    fence_proxy_async();
+    mbar_expect_tx(&bar[b], bytes);
+    stage_span(idx0 + b * L::IDX_BUF, reinterpret_cast<const char *>(J.idx), i0, i1, &bar[b]);
+    stage_span(val0 + b * L::VAL_BUF, reinterpret_cast<const char *>(vplane), v0, v1, &bar[b]);
+  };
+
+  int p = 0;  // polarisation plane of the current (item, plane)
+  while (item < nitems) {
+    const WorkItem w = kp.items[item];
     const JobDesc &J = kp.jobs[w.job];
-    const int N = J.N, G = J.G, log2G = J.log2G;
+    const int N = J.N, log2G = J.log2G;
     const int tx = w.bin % J.ntx, ty = w.bin / J.ntx;
     const int ox = tx * T - H + 1, oy = ty * T - H + 1;  // sub-grid origin
     const int n = w.end - w.start;
-    const bool direct = (long long)n * NRES * 4 < (long long)R * R;
-    const VT2 *vals_base = reinterpret_cast<const VT2 *>(J.vals);
-    GcfSrc<S, GAUSS, VT> gsrc;
-    if constexpr (GAUSS) {
-      gsrc.g1 = g1;
-    } else {
-      gsrc.tab = reinterpret_cast<const VT2 *>(J.gcf);
-      gsrc.G = G;
+    const int nch = (n + K - 1) / K;
+    const bool direct = (long long)n * S * S < (long long)R * R;
+    const int lim = direct ? N : R;
+    // what follows in the stream: the next plane of this item, or the next item
+    const int nxt_item = p + 1 < P ? item : next;
+    const int nxt_p = p + 1 < P ? p + 1 : 0;
+    int nxt_chunks = 0;
+    if (nxt_item < nitems) {
+      const WorkItem w2 = kp.items[nxt_item];
+      nxt_chunks = (w2.end - w2.start + K - 1) / K;
     }
-    const int nchunks = (n + K - 1) / K;
-
-    for (int p = 0; p < P; ++p) {
-      const VT2 *vplane = vals_base + (size_t)p * J.vstride;
-      auto issue = [&](int c, int b) {
-        int s0 = w.start + c * K;
-        int e0 = min(w.end, s0 + K);
-        size_t i0 = (size_t)s0 * 8, i1 = (size_t)e0 * 8;
-        size_t v0 = (size_t)s0 * sizeof(VT2), v1 = (size_t)e0 * sizeof(VT2);
-        uint32_t bytes = (uint32_t)(((i1 + 15) & ~(size_t)15) - (i0 & ~(size_t)15)) +
-                         (uint32_t)(((v1 + 15) & ~(size_t)15) - (v0 & ~(size_t)15));
-        fence_proxy_async();
-        mbar_expect_tx(&bar[b], bytes);
-        stage_span(idxbuf[b], reinterpret_cast<const char *>(J.idx), i0, i1, &bar[b]);
-        stage_span(valbuf[b], reinterpret_cast<const char *>(vplane), v0, v1, &bar[b]);
-      };
-      if (!direct)
-        for (int i = tid; i < R * R; i += NT) region[i] = CellT{};
-      if (tid == 0) {
-        issue(0, 0);
-        if (nchunks > 1) issue(1, 1);
+    auto issue_next = [&](int limit) {
+      while (issued < gfirst + nch + nxt_chunks && issued < limit) {
+        const int c = issued - gfirst;
+        if (c < nch) issue(issued, item, c, p);
+        else issue(issued, nxt_item, c - nch, nxt_p);
+        ++issued;
       }
-      __syncthreads();
+    };
+    if (leader) issue_next(gfirst + 2);
 
-      int cur = -1;
-      ACC acc;
-      acc.zero();
-      auto flush = [&]() {
-        if (direct) out_red_acc(J, (size_t)cur, p, P, acc);
-        else cell_add(region + cur, acc, V == 1);
-      };
-      for (int c = 0; c < nchunks; ++c) {
-        const int b = c & 1;
-        const uint32_t parity = (b == 0 ? uses0 : uses1) & 1;
-        if (!mbar_wait(&bar[b], parity, kp.flags)) s_abort = 1;
-        if (b == 0) ++uses0; else ++uses1;
-        __syncthreads();
-        if (s_abort) break;
-        const int s0 = w.start + c * K;
-        const int m = min(K, w.end - s0);
-        const int2 *ib = reinterpret_cast<const int2 *>(idxbuf[b] + (((size_t)s0 * 8) & 15));
-        const VT2 *vb = reinterpret_cast<const VT2 *>(valbuf[b] + (((size_t)s0 * sizeof(VT2)) & 15));
-        const int r0 = (grp * m) / V, r1 = ((grp + 1) * m) / V;
-        for (int r = r0; r < r1; ++r) {
+    const VT2 *gtab = reinterpret_cast<const VT2 *>(J.gcf);
+    const int G = J.G;
+    ACC acc[Q];
+    int cur[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+      acc[k].zero();
+      cur[k] = -1;
+    }
+
+    for (int c = 0; c < nch; ++c) {
+      const int g = gfirst + c, b = g & 1;
+      if (mbar_wait(&bar[b], (g >> 1) & 1, kp.flags)) waited = g + 1;
+      else s_abort[gid] = 1;
+      group_sync(gid, NGT);
+      if (s_abort[gid]) break;
+      const int s0 = w.start + c * K;
+      const int m = min(K, w.end - s0);
+      const int2 *ib = reinterpret_cast<const int2 *>(idx0 + b * L::IDX_BUF + (((size_t)s0 * 8) & 15));
+      const VT2 *vb = reinterpret_cast<const VT2 *>(val0 + b * L::VAL_BUF +
+                                                    (((size_t)s0 * sizeof(VT2)) & 15));
+      // Two-stage pipeline over the chunk's records: stage A decodes record
+      // r+1 (target cells, value) and issues its GCF loads; stage B adds
+      // record r into the register sums.  The GCF load latency of one record
+      // is hidden behind the accumulation of the previous one.
+      using GT = typename vec2_of<typename ACC::VT>::type;
+      auto run_chunk = [&](auto dir_tag) {
+        constexpr bool D = decltype(dir_tag)::value;  // direct (sparse) item
+        int lcA[Q];
+        GT gA[Q];
+        VT2 vA;
+        auto stageA = [&](int r) {
           const int2 pk = ib[r];
-          const VT2 v = vb[r];
+          vA = vb[r];
           const int mx = unpack_main(pk.x, log2G), sx = unpack_sub(pk.x, log2G);
           const int my = unpack_main(pk.y, log2G), sy = unpack_sub(pk.y, log2G);
           const int fx0 = mx - H + 1, fy0 = my - H + 1;
-          const int ap = (rx - fx0) & (S - 1), bp = (ry - fy0) & (S - 1);
-          const int gx = fx0 + ap, gy = fy0 + bp;
-          bool on = (unsigned)gx < (unsigned)N && (unsigned)gy < (unsigned)N;
-          int lc = -1;
-          if (on) {
-            if (direct) {
-              lc = gy * N + gx;
-            } else {
-              int lx = gx - ox, ly = gy - oy;
-              if ((unsigned)lx < (unsigned)R && (unsigned)ly < (unsigned)R) {
-                lc = ly * R + lx;
-              } else {
-                atomicOr(&kp.flags[FLAG_BOUNDS], 1);
-                on = false;
-              }
+          const int ap = (rx - fx0) & (S - 1);
+          const int lx = fx0 + ap - (D ? 0 : ox);
+          const bool xin = (unsigned)lx < (unsigned)(D ? N : R);
+          const VT2 *gk = GAUSS ? nullptr : gtab + ((sy * G + sx) * S * S + ap);
+          const float gxf = GAUSS ? g1[sx * S + ap] : 0.f;
+#pragma unroll
+          for (int k = 0; k < Q; ++k) {
+            if (S * S % NGT != 0 && !rv[k]) {
+              lcA[k] = -1;
+              continue;
             }
-          }
-          if (lc != cur) {
-            if (cur >= 0) flush();
-            cur = lc;
-            acc.zero();
-          }
-          if (on) {
-            VT gr, gi, tr, ti;
-            gsrc.value(sx, sy, ap, bp, gr, gi);
+            const int bp = (ry[k] - fy0) & (S - 1);
+            const int ly = fy0 + bp - (D ? 0 : oy);
+            lcA[k] = (xin && (unsigned)ly < (unsigned)(D ? N : R)) ? ly * (D ? N : R) + lx : -1;
             if constexpr (GAUSS) {
-              tr = v.x * gr;
-              ti = v.y * gr;
+              gA[k].x = (typename ACC::VT)(gxf * g1[sy * S + bp]);
+              gA[k].y = 0;
             } else {
-              cmul<VT>(v.x, v.y, gr, gi, tr, ti);
+              gA[k] = __ldg(reinterpret_cast<const GT *>(gk) + bp * S);
             }
-            acc.add(tr, ti);
+          }
+        };
+        if (m > 0) stageA(0);
+#pragma unroll 2
+        for (int r = 0; r < m; ++r) {
+          int lcB[Q];
+          GT gB[Q];
+#pragma unroll
+          for (int k = 0; k < Q; ++k) {
+            lcB[k] = lcA[k];
+            gB[k] = gA[k];
+          }
+          const VT2 v = vA;
+          if (r + 1 < m) stageA(r + 1);
+          u64 vv = 0, vrr = 0, vsn = 0;
+          if constexpr (MODE != 2) {
+            vv = pk2((float)v.x, (float)v.y);
+            vrr = pk2((float)v.x, (float)v.x);
+            vsn = pk2(-(float)v.y, (float)v.y);
+          }
+#pragma unroll
+          for (int k = 0; k < Q; ++k) {
+            const int lc = lcB[k];
+            if (lc != cur[k]) {
+              // register sum -> sub-grid (exclusive) or straight to HBM
+              if (cur[k] >= 0) {
+                if (D) acc[k].out(J, (size_t)cur[k], p, P);
+                else acc[k].into(region + cur[k]);
+              }
+              cur[k] = lc;
+              acc[k].zero();
+            }
+            if (lc < 0) continue;
+            if constexpr (MODE == 2) {
+              const double gr = gB[k].x, gi = gB[k].y;
+              acc[k].add(v.x * gr - v.y * gi, v.x * gi + gr * v.y);
+            } else if constexpr (GAUSS) {
+              acc[k].add(mul2(vv, pk2((float)gB[k].x, (float)gB[k].x)));
+            } else {
+              acc[k].add(fma2(vrr, pk2((float)gB[k].x, (float)gB[k].y),
+                              mul2(vsn, pk2((float)gB[k].y, (float)gB[k].x))));
+            }
           }
         }
-        __syncthreads();  // buffer b fully consumed
-        if (tid == 0 && c + 2 < nchunks) issue(c + 2, b);
-      }
-      if (cur >= 0 && !s_abort) flush();
-      __syncthreads();
-      if (!direct && !s_abort) {
-        for (int i = tid; i < R * R; i += NT) {
-          const int gx = ox + i % R, gy = oy + i / R;
-          if ((unsigned)gx >= (unsigned)N || (unsigned)gy >= (unsigned)N) continue;
-          ACC a;
-          cell_load(region[i], a);
-          if (a.nonzero()) out_red_acc(J, (size_t)gy * N + gx, p, P, a);
-        }
-      }
-      __syncthreads();
-      if (s_abort) break;
+      };
+      if (direct) run_chunk(std::true_type{});
+      else run_chunk(std::false_type{});
+      group_sync(gid, NGT);  // buffer b consumed by the whole group
+      if (leader) issue_next(g + 3);
     }
+    if (s_abort[gid]) break;
+#pragma unroll
+    for (int k = 0; k < Q; ++k)
+      if (cur[k] >= 0) {
+        if (direct) acc[k].out(J, (size_t)cur[k], p, P);
+        else acc[k].into(region + cur[k]);
+      }
+    if (!direct) {
+      group_sync(gid, NGT);  // all register sums are in the sub-grid
+      for (int i = gt; i < R * R; i += NGT) {
+        const CellT cv = region[i];
+        if (!cell_nonzero(cv)) continue;
+        region[i] = CellT{};
+        const int gx = ox + i % R, gy = oy + i / R;
+        if ((unsigned)gx < (unsigned)N && (unsigned)gy < (unsigned)N)
+          out_cell(J, (size_t)gy * N + gx, p, P, cv);
+      }
+    }
+    // advance the stream: next plane of this item, or the next item
+    gfirst += nch;
+    if (p + 1 < P) {
+      ++p;
+    } else {
+      p = 0;
+      if (leader) {
+        s_item[gid] = next;
+        s_next[gid] = next < nitems ? atomicAdd(kp.item_next, 1) : nitems;
+      }
+      group_sync(gid, NGT);
+      item = s_item[gid];
+      next = s_next[gid];
+    }
+    group_sync(gid, NGT);  // sub-grid zeroed before the next item's updates
   }
-  // A timed-out copy may still be in flight: drain both barriers (bounded)
-  // before the CTA's shared memory is released.
-  if (s_abort && tid == 0) {
-    mbar_wait(&bar[0], uses0 & 1, nullptr);
-    mbar_wait(&bar[1], uses1 & 1, nullptr);
-  }
+  // A timed-out copy may still be in flight: drain this group's barriers
+  // (bounded) before the CTA's shared memory is released.
+  if (s_abort[gid] && leader)
+    for (int g = waited; g < issued; ++g) mbar_wait(&bar[g & 1], (g >> 1) & 1, nullptr);
 }
 
-size_t window_smem_bytes_t(int S, int accum, int vals_f64, int T) {
-  switch (S) {
-#define GG_WS(SV)                                                        \
-  case SV:                                                               \
-    if (vals_f64) return WinShape<SV, AccF64>::smem(T);                  \
-    if (accum == GG_ACC_COMPENSATED) return WinShape<SV, AccComp>::smem(T); \
-    return WinShape<SV, AccF32>::smem(T);
-    GG_WS(4) GG_WS(8) GG_WS(16) GG_WS(32)
-#undef GG_WS
-  }
-  return 0;
-}
-
-template <int S, class ACC, bool GAUSS>
+template <int S, int W, int MODE, bool GAUSS>
 static cudaError_t win_launch(const KParams &kp, int sm_count, cudaStream_t s) {
-  using Sh = WinShape<S, ACC>;
-  size_t smem = Sh::smem(kp.T);
-  auto kern = window_kernel<S, ACC, GAUSS>;
+  using L = WinLayout<S, W, MODE>;
+  const size_t smem = L::cta_bytes(kp.T);
+  auto kern = window_kernel<S, W, MODE, GAUSS>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Sh::NT, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWinThreads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  kern<<<sm_count * per_sm, Sh::NT, smem, s>>>(kp);
+  kern<<<sm_count * per_sm, kWinThreads, smem, s>>>(kp);
   count_launch();
   return cudaGetLastError();
 }
 
-template <int S>
-static cudaError_t win_dispatch(const GridLaunch &g, const KParams &kp,
-                                cudaStream_t s) {
+template <int S, int W>
+static cudaError_t win_modes(const GridLaunch &g, const KParams &kp, cudaStream_t s) {
   if (g.vals_f64)
-    return g.gauss ? win_launch<S, AccF64, true>(kp, g.sm_count, s)
-                   : win_launch<S, AccF64, false>(kp, g.sm_count, s);
+    return g.gauss ? win_launch<S, W, 2, true>(kp, g.sm_count, s)
+                   : win_launch<S, W, 2, false>(kp, g.sm_count, s);
   if (g.accum == GG_ACC_COMPENSATED)
-    return g.gauss ? win_launch<S, AccComp, true>(kp, g.sm_count, s)
-                   : win_launch<S, AccComp, false>(kp, g.sm_count, s);
-  return g.gauss ? win_launch<S, AccF32, true>(kp, g.sm_count, s)
-                 : win_launch<S, AccF32, false>(kp, g.sm_count, s);
+    return g.gauss ? win_launch<S, W, 1, true>(kp, g.sm_count, s)
+                   : win_launch<S, W, 1, false>(kp, g.sm_count, s);
+  return g.gauss ? win_launch<S, W, 0, true>(kp, g.sm_count, s)
+                 : win_launch<S, W, 0, false>(kp, g.sm_count, s);
+}
+
+// supported (support, warps per group): Q = S*S/(32 W) residues per thread
+// between 1 and 8
+static int win_warps(int S, int requested) {
+  int w = requested > 0 ? requested : win_default_warps(S);
+  switch (S) {
+    case 4: return 1;
+    case 8: return w >= 2 ? 2 : 1;
+    case 16: return w >= 4 ? 4 : (w >= 2 ? 2 : 1);
+    case 32: return w >= 8 ? 8 : 4;
+  }
+  return w;
+}
+
+size_t window_smem_bytes(int S, int accum, int vals_f64, int T, int group_warps) {
+  const int mode = vals_f64 ? 2 : (accum == GG_ACC_COMPENSATED ? 1 : 0);
+  const int w = win_warps(S, group_warps);
+#define GG_WS(SV, WV)                                                      \
+  return mode == 2 ? WinLayout<SV, WV, 2>::cta_bytes(T)                    \
+                   : (mode == 1 ? WinLayout<SV, WV, 1>::cta_bytes(T)       \
+                                : WinLayout<SV, WV, 0>::cta_bytes(T))
+  switch (S) {
+    case 4: GG_WS(4, 1);
+    case 8:
+      if (w == 2) GG_WS(8, 2);
+      GG_WS(8, 1);
+    case 16:
+      if (w == 4) GG_WS(16, 4);
+      if (w == 2) GG_WS(16, 2);
+      GG_WS(16, 1);
+    case 32:
+      if (w == 8) GG_WS(32, 8);
+      GG_WS(32, 4);
+  }
+#undef GG_WS
+  return 0;
 }
 
 cudaError_t launch_window(const GridLaunch &g, cudaStream_t s) {
@@ -322,11 +530,14 @@ cudaError_t launch_window(const GridLaunch &g, cudaStream_t s) {
   kp.T = g.tile;
   kp.G = g.G;
   kp.sigma = g.sigma;
+  const int w = win_warps(g.S, g.group_warps);
   switch (g.S) {
-    case 4: return win_dispatch<4>(g, kp, s);
-    case 8: return win_dispatch<8>(g, kp, s);
-    case 16: return win_dispatch<16>(g, kp, s);
-    case 32: return win_dispatch<32>(g, kp, s);
+    case 4: return win_modes<4, 1>(g, kp, s);
+    case 8: return w == 2 ? win_modes<8, 2>(g, kp, s) : win_modes<8, 1>(g, kp, s);
+    case 16:
+      return w == 4 ? win_modes<16, 4>(g, kp, s)
+                    : (w == 2 ? win_modes<16, 2>(g, kp, s) : win_modes<16, 1>(g, kp, s));
+    case 32: return w == 8 ? win_modes<32, 8>(g, kp, s) : win_modes<32, 4>(g, kp, s);
   }
   return cudaErrorInvalidValue;
 }

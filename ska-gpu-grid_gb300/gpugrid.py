@@ -54,7 +54,8 @@ class gg_options(ctypes.Structure):
                 ("input_sorted", ctypes.c_int32),
                 ("gcf_sigma", ctypes.c_double),
                 ("window_chunk", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 7)]
+                ("group_warps", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
 
 
 class gg_job(ctypes.Structure):
@@ -124,10 +125,11 @@ class Options:
     gcf_kind: int = GCF_TABLE           # COMPUTE_GCF=1 -> GCF_GAUSSIAN
     oversample: int = 8                 # GCF_GRID
     polarizations: int = 1              # POLARIZATIONS
-    tile: int = 32
+    tile: int = 0                       # 0: chosen by method and support
     input_sorted: bool = False
     gcf_sigma: float = 0.0
     window_chunk: int = 0
+    group_warps: int = 0                # moving window: warps per sub-grid
 
     def c(self) -> gg_options:
         o = gg_options()
@@ -137,6 +139,7 @@ class Options:
         o.oversample, o.polarizations, o.tile = self.oversample, self.polarizations, self.tile
         o.input_sorted = int(bool(self.input_sorted))
         o.gcf_sigma, o.window_chunk = self.gcf_sigma, self.window_chunk
+        o.group_warps = self.group_warps
         return o
 
 

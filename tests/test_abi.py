@@ -73,7 +73,7 @@ def test_abi_version_and_defaults():
     assert gg.LIB.gg_default_options(ctypes.byref(o)) == gg.OK
     assert (o.mode, o.layout, o.accum, o.gcf_kind) == (
         gg.MODE_SCATTER, gg.LAYOUT_REFERENCE, gg.ACC_PLAIN, gg.GCF_TABLE)
-    assert (o.oversample, o.polarizations, o.tile) == (8, 1, 32)
+    assert (o.oversample, o.polarizations, o.tile) == (8, 1, 0)
 
 
 @pytest.mark.parametrize("field,value", [
