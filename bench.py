@@ -4,22 +4,37 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
                     [--impl ours|reference]
 
-A step is one gridding pass over one batch of synthetic visibilities with the
-inputs resident in HBM (value), or, for e2e, the same pass through the C ABI
-(gg_grid_host) from pinned host buffers, host->device copies and the
-device->host grid copy included.  L2 is flushed (256 MiB write) before every
-timed step; steps are timed with CUDA events on the launching stream.
+Workloads (seeded synthetic visibilities with each configuration's shapes):
+
+  served10k   (default) a stream of 10,000 gridding requests -- grid side
+              uniform in {256,512,1024,2048}, support 8 or 16, visibility count
+              lognormal in [1e4, 1e6], uv tracks -- through the request server
+              (HBM-budget admission, continuous batching over CUDA streams,
+              grids and GCF tables resident).  A step = the whole stream
+              submitted at once (saturation); an arrival-rate sweep (Poisson)
+              reports p50/p99 latency; the same stream through plain per-request
+              launches is timed for comparison.
+  batch256    256 such jobs in one batched plan captured in a CUDA graph.
+  tracks4096  one 4096^2 job, 2^22 visibilities on uv tracks, support 8.
+  uniform1024 one 1024^2 FP64 job, 2^18 uniform visibilities, support 16.
+  disk8192    one 8192^2 job, 2^24 visibilities in a disk with 1% outliers,
+              support 32, GCF computed on the fly.
+
+`value` is Mvis/s with the inputs resident in HBM; `e2e` is the same metric
+with the inputs copied from pinned host memory and the grids copied back,
+inside the timed region, through the library's public API.
 
 --impl reference times the reference's CPU gridder (gridCPU_pz, grid.cu:
-140-193) on the host cores: the C restatement in oracle/ split over all host
-threads in row bands (bit-identical to the single-threaded reference), on a
-bounded sample of the same workload.
-Under torchrun each rank grids its own replica of the workload (independent
-jobs, weak scaling); rank 0 prints the line with the max time over ranks.
+140-193) on the host cores -- the C restatement in oracle/ split over all
+host threads in row bands, bit-identical to the single-threaded reference --
+on a bounded sample of the same workload.
+Under torchrun each rank runs its own replica (independent jobs, weak
+scaling); rank 0 prints the line with the max time over ranks.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -38,68 +53,54 @@ METRIC = ("gridded Mvis/s batched+served vs plain kernel at <=1e-6 rel err; "
           "p50/p99 latency")
 FALLBACK_HBM_GBS = 6800.0
 
+STREAM_DESC = ("grid side uniform in {256,512,1024,2048}; support 8 or 16, "
+               "oversample 8; visibility count lognormal (log10 ~ N(5, 0.5)) "
+               "clipped to [1e4, 1e6]; each a slice of one of 8 synthetic "
+               "uv-track observations per grid side (64 antennas in a 2 km "
+               "disk, dec -30 deg, 90% fill); complex64 N(0,1) values; FP64 "
+               "u,v; complex64 grids; FP32 compensated accumulation; "
+               "tabulated separable Gaussian GCFs resident on the device")
+
 WORKLOADS = {
-    # gather / moving-window workload
+    "served10k": dict(kind="served", n=10000, streams=3, max_batch_jobs=512,
+                      max_batch_vis=1 << 26, budget=150e9,
+                      desc="10,000 Poisson-arrival gridding requests: " + STREAM_DESC +
+                           "; HBM admission budget 150 GB"),
+    "batch256": dict(kind="batch", n=256,
+                     desc="256 independent gridding jobs in one batched "
+                          "launch captured in a CUDA graph: " + STREAM_DESC),
     "tracks4096": dict(
-        N=4096, S=8, npts=1 << 22, gen="tracks", vals="c64", out="c64",
-        mode="auto", accum="comp", presort=True, input_sorted=False,
+        kind="single", N=4096, S=8, npts=1 << 22, gen="tracks", vals="c64", out="c64",
+        mode="auto", accum="comp", presort=True,
         desc=("4096^2 complex64 grid; 2^22 visibilities on uv tracks (64 "
               "antennas in a 2 km disk, 2016 baselines x 2080 hour angles over "
               "+-4 h at dec -30 deg, 90% fill, +1024 to 2^22); complex64 N(0,1) "
               "values; FP64 u,v; support 8, oversample 8; presorted into 32x32 "
               "uv tiles; FP32 compensated accumulation")),
-    # plain scatter workload (FP64, the CPU-reference-runs case)
     "uniform1024": dict(
-        N=1024, S=16, npts=1 << 18, gen="uniform", vals="c128", out="c128",
-        mode="scatter", accum="plain", input_sorted=False,
+        kind="single", N=1024, S=16, npts=1 << 18, gen="uniform", vals="c128", out="c128",
+        mode="scatter", accum="plain",
         desc=("1024^2 complex128 grid; 2^18 visibilities uniform in "
               "[16, 1008); complex128 N(0,1) values; support 16, oversample 8; "
               "FP64 scatter")),
-    # precision workload
     "disk8192": dict(
-        N=8192, S=32, npts=1 << 24, gen="disk", vals="c64", out="c128",
-        mode="auto", accum="comp", input_sorted=False, gcf="gauss",
+        kind="single", N=8192, S=32, npts=1 << 24, gen="disk", vals="c64", out="c128",
+        mode="auto", accum="comp", gcf="gauss",
         desc=("8192^2 grid (complex128 output of FP32 compensated "
               "accumulation); 2^24 visibilities, uniform disk; N(0,1) values "
               "with 1% outliers at 1e3; support 32, oversample 8; GCF computed "
               "on the fly")),
 }
+DEFAULT_WORKLOAD = "served10k"
 
 
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-# ---------------------------------------------------------------------------
-# inputs
-# ---------------------------------------------------------------------------
-def make_inputs(w, seed):
-    import synth
-    N, S, n = w["N"], w["S"], w["npts"]
-    vdt = np.complex64 if w["vals"] == "c64" else np.complex128
-    if w["gen"] == "tracks":
-        uv, vals = synth.tracks(N, npts=n, seed=seed, vals_dtype=vdt)
-    elif w["gen"] == "disk":
-        uv, vals = synth.disk(n, N, seed=seed, outlier_frac=0.01, vals_dtype=vdt)
-    else:
-        uv, vals = synth.uniform(n, S, N - S, seed=seed, vals_dtype=vdt)
-    if w.get("presort"):
-        # the data format of the workload: grouped into 32x32 uv tiles; the
-        # gridder still bins on the device at its own tile size
-        perm = synth.tile_sort(uv, N, 32)
-        uv, vals = np.ascontiguousarray(uv[perm]), np.ascontiguousarray(vals[perm])
-    g1 = synth.gaussian_gcf_1d(S)
-    gcf = synth.gcf_table(g1).astype(vdt)
-    return uv, vals, gcf
-
-
-def options(w):
-    import gpugrid as gg
-    return gg.Options(
-        mode=gg.MODES[w["mode"]],
-        accum=gg.ACC_COMPENSATED if w["accum"] == "comp" else gg.ACC_PLAIN,
-        gcf_kind=gg.GCF_GAUSSIAN if w.get("gcf") == "gauss" else gg.GCF_TABLE,
-        layout=gg.LAYOUT_INTERLEAVED, input_sorted=w.get("input_sorted", False))
+def pairs(c):
+    c = np.asarray(c).reshape(-1)
+    return np.stack([c.real, c.imag], -1).astype(np.float64)
 
 
 # ---------------------------------------------------------------------------
@@ -162,19 +163,17 @@ class ClockSampler:
 
 
 def peaks():
-    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
-        d = json.load(open(p))
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def traffic_from_profile(kernel_tag):
+def traffic_from_profile(tag):
     """dram bytes per launch recorded from an ncu capture (profiles/)."""
-    p = os.path.join(ROOT, "profiles", f"{kernel_tag}.txt")
     try:
-        for line in open(p):
+        for line in open(os.path.join(ROOT, "profiles", f"{tag}.txt")):
             if line.startswith("traffic_bytes_per_launch:"):
                 return float(line.split(":")[1])
     except OSError:
@@ -182,32 +181,505 @@ def traffic_from_profile(kernel_tag):
     return None
 
 
+def roofline(kernel, alg_bytes, kern_ms, tag):
+    hbm, kind = peaks()
+    achieved = alg_bytes / (kern_ms / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": hbm,
+            "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_kind": f"{kind} (copy)",
+            "traffic": traffic_from_profile(tag), "algorithmic_bytes_per_launch": int(alg_bytes)}
+
+
 # ---------------------------------------------------------------------------
-# CPU baseline (oracle restatement of gridCPU_pz)
+# CPU baseline: the oracle restatement of gridCPU_pz on the host cores
 # ---------------------------------------------------------------------------
-def cpu_grid_rate(w, uv, vals, gcf, budget_s=8.0, threads=None):
-    """Mvis/s of the CPU gridder on a bounded sample, all host threads."""
+def cpu_rate(jobs, budget_s, threads=None):
+    """jobs: list of (uv, vals, gcf, N, S).  Grids jobs until about budget_s
+    seconds have been spent; returns (Mvis/s, visibilities, seconds)."""
     import oracle as O
     threads = threads or os.cpu_count() or 1
-    N, S = w["N"], w["S"]
-    pairs = lambda c: np.stack([c.real, c.imag], -1).astype(np.float64).reshape(-1, 2)
-    g = pairs(gcf.reshape(-1))
-    n = min(len(uv), 1 << 14)
-    t0 = time.perf_counter()
-    O.grid_pz(uv[:n], pairs(vals[:n]), g, N, S, nthreads=threads)
-    dt = time.perf_counter() - t0
-    per = dt / n
-    n2 = int(min(len(uv), max(n, budget_s / max(per, 1e-12))))
-    t0 = time.perf_counter()
-    O.grid_pz(uv[:n2], pairs(vals[:n2]), g, N, S, nthreads=threads)
-    dt = time.perf_counter() - t0
-    return n2 / dt / 1e6, n2, dt, threads
+    vis, spent = 0, 0.0
+    for uv, vals, gcf, N, S in jobs:
+        t0 = time.perf_counter()
+        O.grid_pz(uv, pairs(vals), pairs(gcf), N, S, nthreads=threads)
+        spent += time.perf_counter() - t0
+        vis += len(uv)
+        if spent >= budget_s:
+            break
+    return vis / spent / 1e6, vis, spent, threads
 
 
 # ---------------------------------------------------------------------------
-# our arm
+# shared pieces of the batched and served workloads
 # ---------------------------------------------------------------------------
-def run_ours(args, rank, world, local_rank, dist):
+def stream_inputs(n, seed):
+    import synth
+    pools = synth.track_pool(seed=seed)
+    specs = synth.request_specs(n, seed=seed + 1)
+    gcfs = {S: synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64) for S in (8, 16)}
+    return pools, specs, gcfs
+
+
+def slice_of(pools, specs, i):
+    N, s, off, n = (int(specs[k][i]) for k in ("side", "set", "offset", "nvis"))
+    uv, vals = pools[N]
+    return uv[s, off:off + n], vals[s, off:off + n]
+
+
+class DevicePools:
+    """track pools on the device; pointers into them for each request"""
+
+    def __init__(self, pools, dev):
+        import torch
+        self.t = {N: (torch.from_numpy(uv).to(dev), torch.from_numpy(v).to(dev))
+                  for N, (uv, v) in pools.items()}
+        self.len = {N: uv.shape[1] for N, (uv, _) in pools.items()}
+
+    def ptrs(self, N, s, off):
+        uv, v = self.t[N]
+        L = self.len[N]
+        return (uv.data_ptr() + (s * L + off) * 16, v.data_ptr() + (s * L + off) * 8)
+
+
+def check_sample(grids, pools, specs, gcfs, idx):
+    """max / RMS relative error of device grids vs the FP64 oracle"""
+    import oracle as O
+    worst, rms_num, rms_den = 0.0, 0.0, 0.0
+    for i, g in zip(idx, grids):
+        uv, vals = slice_of(pools, specs, i)
+        N, S = int(specs["side"][i]), int(specs["S"][i])
+        ref = O.grid_pz(uv, pairs(vals), pairs(gcfs[S]), N, S, nthreads=os.cpu_count())
+        got = np.stack([g.real, g.imag]).reshape(2, 1, N, N).astype(np.float64)
+        worst = max(worst, float(np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300)))
+        rms_num += float(((got - ref) ** 2).sum())
+        rms_den += float((ref ** 2).sum())
+    return {"max_rel": worst, "rms_rel": (rms_num / max(rms_den, 1e-300)) ** 0.5,
+            "jobs_checked": len(idx), "reference": "FP64 oracle (gridCPU_pz restatement)"}
+
+
+def cudart():
+    f = ctypes.CDLL("libcudart.so.13")
+    f.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+    f.cudaMemcpy.restype = ctypes.c_int
+    return f
+
+
+# ---------------------------------------------------------------------------
+# served stream (config 5) -- the headline
+# ---------------------------------------------------------------------------
+def run_served(args, rank, world, local_rank, dist):
+    import torch
+    import gpugrid as gg
+    w = WORKLOADS[args.workload]
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    n = w["n"]
+    pools, specs, gcfs = stream_inputs(n, seed=7 + rank)
+    total_vis = int(specs["nvis"].sum())
+    dp = DevicePools(pools, dev)
+    opts = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
+                      layout=gg.LAYOUT_INTERLEAVED)
+    srv = gg.Server(device=local_rank, streams=w["streams"], max_batch_jobs=w["max_batch_jobs"],
+                    max_batch_vis=w["max_batch_vis"], hbm_budget=w["budget"], options=opts)
+    gids = {S: srv.add_gcf(gcfs[S]) for S in (8, 16)}
+    flags = gg.REQ_INPUTS_ON_DEVICE | gg.REQ_KEEP_RESIDENT
+    reqs = []
+    for i in range(n):
+        N, S = int(specs["side"][i]), int(specs["S"][i])
+        pu, pv = dp.ptrs(N, int(specs["set"][i]), int(specs["offset"][i]))
+        reqs.append(gg.Server.request(pu, pv, None, int(specs["nvis"][i]), N, S, gids[S],
+                                      flags=flags))
+
+    def stream(offsets, keep=()):
+        """submit all requests at the given arrival offsets; wait, release;
+        returns (server span seconds, stats, kept grids)"""
+        srv.stats(reset=True)
+        tickets = srv.submit_schedule(reqs, offsets)
+        kept = {}
+        for k, t in enumerate(tickets):
+            r = srv.wait(int(t), timeout=600)
+            if k in keep:
+                N = int(specs["side"][k])
+                h = np.empty(N * N, np.complex64)
+                cudart().cudaMemcpy(h.ctypes.data, ctypes.c_void_p(r.device_out), h.nbytes, 2)
+                kept[k] = h
+            srv.release(int(t))
+        st = srv.stats()
+        return st["span_s"], st, kept
+
+    zeros = np.zeros(n)
+    for _ in range(args.warmup):
+        stream(zeros)
+    # timed saturation passes (all arrivals at t=0); L2: the 768 MB of input
+    # pools exceed it
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = gg.kernel_launches()
+    spans, stats = [], []
+    with ClockSampler(local_rank) as clk:
+        for _ in range(args.steps):
+            span, st, _ = stream(zeros)
+            spans.append(span)
+            stats.append(st)
+        torch.cuda.synchronize()
+    launches = gg.kernel_launches() - l0
+    total_s = sum(spans)
+    if dist:
+        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * total_vis * args.steps / total_s / 1e6
+
+    # arrival-rate sweep (Poisson) up to saturation
+    rng = np.random.default_rng(11)
+    cap_rps = n / (total_s / args.steps)
+    sweep = []
+    for frac in (0.25, 0.5, 0.75, 0.9):
+        rate = frac * cap_rps
+        offs = np.cumsum(rng.exponential(1.0 / rate, n))
+        span, st, _ = stream(offs)
+        sweep.append({"load": frac, "rate_req_per_s": round(rate, 1),
+                      "Mvis_per_s": round(total_vis / span / 1e6, 1),
+                      "p50_ms": round(1e3 * st["p50_latency_s"], 3),
+                      "p99_ms": round(1e3 * st["p99_latency_s"], 3),
+                      "mean_batch_jobs": round(st["mean_batch_jobs"], 2)})
+    sat = stats[-1]
+    sweep.append({"load": "saturation (all at t=0)", "Mvis_per_s": round(value / world, 1),
+                  "p50_ms": round(1e3 * sat["p50_latency_s"], 3),
+                  "p99_ms": round(1e3 * sat["p99_latency_s"], 3),
+                  "mean_batch_jobs": round(sat["mean_batch_jobs"], 2)})
+
+    # accuracy on a sample of requests, from the server's resident grids
+    sample = list(range(0, n, max(1, n // 12)))[:12]
+    _, _, kept = stream(zeros, keep=set(sample))
+    acc = check_sample([kept[i] for i in sample], pools, specs, gcfs, sample) \
+        if rank == 0 and not args.no_check else None
+
+    # plain per-request launches on one stream (no batching)
+    ctx = gg.Context(local_rank)
+    outs = {N: torch.empty(N * N, dtype=torch.complex64, device=dev) for N in (256, 512, 1024, 2048)}
+    dg = {S: torch.from_numpy(gcfs[S].reshape(-1)).to(dev) for S in (8, 16)}
+    plain = {}
+    for label, o in (("plain_scatter_per_request",
+                      gg.Options(mode=gg.MODE_SCATTER, accum=gg.ACC_PLAIN,
+                                 layout=gg.LAYOUT_INTERLEAVED)),
+                     ("window_per_request", opts)):
+        jobs = []
+        for i in range(n):
+            N, S = int(specs["side"][i]), int(specs["S"][i])
+            pu, pv = dp.ptrs(N, int(specs["set"][i]), int(specs["offset"][i]))
+            j = gg.gg_job()
+            j.out, j.uv, j.vals, j.gcf = outs[N].data_ptr(), pu, pv, dg[S].data_ptr()
+            j.npts, j.img_dim, j.gcf_dim = int(specs["nvis"][i]), N, S
+            j.uv_type, j.vals_type, j.out_type = gg.C128, gg.C64, gg.C64
+            jobs.append(j)
+        for j in jobs[:50]:
+            ctx.grid_job(o, j)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for j in jobs:
+            ctx.grid_job(o, j)
+        e1.record()
+        torch.cuda.synchronize()
+        plain[label] = round(total_vis / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
+
+    # kernel-level roofline: the first 256 requests as one profiled batch
+    ctx.profile(True)
+    jobs = []
+    grid_out = {}
+    for i in range(min(256, n)):
+        N, S = int(specs["side"][i]), int(specs["S"][i])
+        pu, pv = dp.ptrs(N, int(specs["set"][i]), int(specs["offset"][i]))
+        grid_out[i] = torch.empty(N * N, dtype=torch.complex64, device=dev)
+        j = gg.gg_job()
+        j.out, j.uv, j.vals, j.gcf = grid_out[i].data_ptr(), pu, pv, dg[S].data_ptr()
+        j.npts, j.img_dim, j.gcf_dim = int(specs["nvis"][i]), N, S
+        j.uv_type, j.vals_type, j.out_type = gg.C128, gg.C64, gg.C64
+        jobs.append(j)
+    for _ in range(3):
+        ctx.grid_batch(opts, jobs)
+    ctx.grid_batch(opts, jobs)
+    _, kern_ms, _ = ctx.profile_last()
+    nv = sum(j.npts for j in jobs)
+    alg = nv * 16 + sum(2 * 8 * j.img_dim * j.img_dim for j in jobs)
+    roof = roofline("window_kernel", alg, kern_ms, "window_batch256")
+
+    # e2e: inputs from pinned host memory through the server, grids read back
+    e2e = None
+    if not args.no_e2e:
+        import torch as _t
+        hp = {N: (_t.from_numpy(uv).pin_memory().numpy(), _t.from_numpy(v).pin_memory().numpy())
+              for N, (uv, v) in pools.items()}
+        hout = {N: _t.empty(N * N, dtype=_t.complex64).pin_memory().numpy() for N in hp}
+        hreqs = []
+        for i in range(n):
+            N, S = int(specs["side"][i]), int(specs["S"][i])
+            s_, off, nv_ = int(specs["set"][i]), int(specs["offset"][i]), int(specs["nvis"][i])
+            uvh, vh = hp[N]
+            L = uvh.shape[1]
+            hreqs.append(gg.Server.request(uvh.ctypes.data + (s_ * L + off) * 16,
+                                           vh.ctypes.data + (s_ * L + off) * 8, None, nv_, N, S,
+                                           gids[S], flags=gg.REQ_KEEP_RESIDENT))
+        cr = cudart()
+        t_all = 0.0
+        for _ in range(max(1, min(args.steps, 3))):
+            srv.stats(reset=True)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            tickets = srv.submit_schedule(hreqs, zeros)
+            for k, t in enumerate(tickets):
+                r = srv.wait(int(t), timeout=600)
+                N = int(specs["side"][k])
+                cr.cudaMemcpy(hout[N].ctypes.data, ctypes.c_void_p(r.device_out),
+                              hout[N].nbytes, 2)
+                srv.release(int(t))
+            t_all += time.perf_counter() - t0
+        reps = max(1, min(args.steps, 3))
+        e2e = {"value": round(world * total_vis * reps / t_all / 1e6, 3), "unit": "Mvis/s",
+               "h2d_bytes_per_step": int(total_vis * 24),
+               "d2h_bytes_per_step": int(sum(8 * int(N) * int(N) for N in specs["side"])),
+               "ms_per_step": round(1e3 * t_all / reps, 3),
+               "api": "gg_server_* (C ABI): inputs from pinned host memory, each grid "
+                      "copied back to the host"}
+    srv.close()
+
+    if rank != 0:
+        return None
+    cpu_jobs = []
+    for i in range(60):
+        uv, vals = slice_of(pools, specs, i)
+        cpu_jobs.append((uv, vals, gcfs[int(specs["S"][i])], int(specs["side"][i]),
+                         int(specs["S"][i])))
+    cv, cn, cs, ct = cpu_rate(cpu_jobs, args.cpu_budget)
+    best_plain = max(plain.values())
+    res = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mvis/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * total_s / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generators with the workload's shapes)",
+        "config": {"workload": f"{args.workload}: {w['desc']}",
+                   "visibilities_per_step": total_vis, "requests": n,
+                   "server": {"streams": w["streams"], "max_batch_jobs": w["max_batch_jobs"],
+                              "hbm_budget_bytes": int(w["budget"]), "method": "window"},
+                   "l2": "inputs (768 MB of track pools) exceed L2",
+                   "timing": "server clock from first arrival to last grid ready, "
+                             "per pass; device synchronised around the passes",
+                   "parallelism": f"replicas x{world}"},
+        "plain_per_request_Mvis_per_s": plain,
+        "speedup_vs_best_plain": round(value / world / best_plain, 2),
+        "latency_sweep": sweep,
+        "accuracy": acc,
+        "roofline": roof,
+        "cpu_baseline": {"value": round(cv, 4), "unit": "Mvis/s", "cores": ct, "kind": "port",
+                         "sample": f"first requests of the stream, {cn} visibilities "
+                                   f"({cs:.1f} s), gridCPU_pz restatement over {ct} row bands"},
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+    }
+    clocks = clk.summary()
+    if clocks:
+        res["clocks"] = clocks
+    return res
+
+
+# ---------------------------------------------------------------------------
+# batched plan in a CUDA graph (config 4)
+# ---------------------------------------------------------------------------
+def run_batch(args, rank, world, local_rank, dist):
+    import torch
+    import gpugrid as gg
+    w = WORKLOADS[args.workload]
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    n = w["n"]
+    pools, specs, gcfs = stream_inputs(n, seed=17 + rank)
+    total_vis = int(specs["nvis"].sum())
+    dp = DevicePools(pools, dev)
+    dg = {S: torch.from_numpy(gcfs[S].reshape(-1)).to(dev) for S in (8, 16)}
+    opts = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
+                      layout=gg.LAYOUT_INTERLEAVED)
+    outs, jobs = [], []
+    for i in range(n):
+        N, S = int(specs["side"][i]), int(specs["S"][i])
+        pu, pv = dp.ptrs(N, int(specs["set"][i]), int(specs["offset"][i]))
+        o = torch.empty(N * N, dtype=torch.complex64, device=dev)
+        outs.append(o)
+        j = gg.gg_job()
+        j.out, j.uv, j.vals, j.gcf = o.data_ptr(), pu, pv, dg[S].data_ptr()
+        j.npts, j.img_dim, j.gcf_dim = int(specs["nvis"][i]), N, S
+        j.uv_type, j.vals_type, j.out_type = gg.C128, gg.C64, gg.C64
+        jobs.append(j)
+    ctx = gg.Context(local_rank)
+    plan = gg.Plan(ctx, opts, jobs)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        plan.launch(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        plan.launch(s)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        g.replay()
+    torch.cuda.synchronize()
+    flags = plan.read_flags()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = gg.kernel_launches()
+    cs = torch.cuda.current_stream()
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)
+            ev[k][0].record(cs)
+            g.replay()
+            ev[k][1].record(cs)
+        torch.cuda.synchronize()
+    # graph replays launch the captured kernels without the library's counter
+    launches = (gg.kernel_launches() - l0) or None
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if dist:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * total_vis * args.steps / (total_ms / 1e3) / 1e6
+    # number of kernels in one replay: count a direct (uncaptured) launch
+    l1 = gg.kernel_launches()
+    plan.launch()
+    torch.cuda.synchronize()
+    per_step = gg.kernel_launches() - l1
+    launches = per_step * args.steps
+    # accuracy on a sample of jobs
+    sample = list(range(0, n, max(1, n // 12)))[:12]
+    acc = check_sample([outs[i].cpu().numpy() for i in sample], pools, specs, gcfs, sample) \
+        if rank == 0 and not args.no_check else None
+    # plain per-job launches
+    plain = {}
+    for label, o in (("plain_scatter_per_job",
+                      gg.Options(mode=gg.MODE_SCATTER, accum=gg.ACC_PLAIN,
+                                 layout=gg.LAYOUT_INTERLEAVED)),
+                     ("window_per_job", opts)):
+        for j in jobs[:20]:
+            ctx.grid_job(o, j)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for j in jobs:
+            ctx.grid_job(o, j)
+        e1.record()
+        torch.cuda.synchronize()
+        plain[label] = round(total_vis / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
+    ctx.profile(True)
+    ctx.grid_batch(opts, jobs)
+    ctx.grid_batch(opts, jobs)
+    _, kern_ms, _ = ctx.profile_last()
+    alg = total_vis * 16 + sum(2 * 8 * j.img_dim * j.img_dim for j in jobs)
+    roof = roofline("window_kernel", alg, kern_ms, "window_batch256")
+    # e2e through the server's host path: one batch of host requests
+    e2e = None
+    if not args.no_e2e:
+        hp = {N: (torch.from_numpy(uv).pin_memory().numpy(), torch.from_numpy(v).pin_memory().numpy())
+              for N, (uv, v) in pools.items()}
+        houts = [torch.empty(int(N) * int(N), dtype=torch.complex64).pin_memory().numpy()
+                 for N in specs["side"]]
+        srv = gg.Server(device=local_rank, streams=1, max_batch_jobs=n, options=opts)
+        gids = {S: srv.add_gcf(gcfs[S]) for S in (8, 16)}
+        reqs = []
+        for i in range(n):
+            N, S = int(specs["side"][i]), int(specs["S"][i])
+            s_, off, nv_ = int(specs["set"][i]), int(specs["offset"][i]), int(specs["nvis"][i])
+            uvh, vh = hp[N]
+            L = uvh.shape[1]
+            reqs.append(gg.Server.request(uvh.ctypes.data + (s_ * L + off) * 16,
+                                          vh.ctypes.data + (s_ * L + off) * 8,
+                                          houts[i].ctypes.data, nv_, N, S, gids[S]))
+        zeros = np.zeros(n)
+        for _ in range(2):
+            for t in srv.submit_schedule(reqs, zeros):
+                srv.wait(int(t), timeout=600)
+                srv.release(int(t))
+        reps = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            for t in srv.submit_schedule(reqs, zeros):
+                srv.wait(int(t), timeout=600)
+                srv.release(int(t))
+        t_all = time.perf_counter() - t0
+        srv.close()
+        e2e = {"value": round(world * total_vis * reps / t_all / 1e6, 3), "unit": "Mvis/s",
+               "h2d_bytes_per_step": int(total_vis * 24),
+               "d2h_bytes_per_step": int(sum(8 * int(N) * int(N) for N in specs["side"])),
+               "ms_per_step": round(1e3 * t_all / reps, 3),
+               "api": "gg_server_* (C ABI) with host input and output buffers"}
+    if rank != 0:
+        return None
+    cpu_jobs = []
+    for i in range(40):
+        uv, vals = slice_of(pools, specs, i)
+        cpu_jobs.append((uv, vals, gcfs[int(specs["S"][i])], int(specs["side"][i]),
+                         int(specs["S"][i])))
+    cv, cn, cs_, ct = cpu_rate(cpu_jobs, args.cpu_budget)
+    res = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mvis/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generators with the workload's shapes)",
+        "config": {"workload": f"{args.workload}: {w['desc']}",
+                   "visibilities_per_step": total_vis, "jobs": n,
+                   "l2": "flushed before every timed step (256 MiB write)",
+                   "launch": "one gg_plan_launch captured in a CUDA graph, replayed",
+                   "parallelism": f"replicas x{world}"},
+        "plain_per_job_Mvis_per_s": plain,
+        "speedup_vs_best_plain": round(value / world / max(plain.values()), 2),
+        "flags": flags, "accuracy": acc, "roofline": roof,
+        "cpu_baseline": {"value": round(cv, 4), "unit": "Mvis/s", "cores": ct, "kind": "port",
+                         "sample": f"first jobs, {cn} visibilities ({cs_:.1f} s), gridCPU_pz "
+                                   f"restatement over {ct} row bands"},
+        "e2e": e2e, "gpu_launches": int(launches),
+    }
+    clocks = clk.summary()
+    if clocks:
+        res["clocks"] = clocks
+    return res
+
+
+# ---------------------------------------------------------------------------
+# single job (configs 1-3)
+# ---------------------------------------------------------------------------
+def make_single(w, seed):
+    import synth
+    N, S, n = w["N"], w["S"], w["npts"]
+    vdt = np.complex64 if w["vals"] == "c64" else np.complex128
+    if w["gen"] == "tracks":
+        uv, vals = synth.tracks(N, npts=n, seed=seed, vals_dtype=vdt)
+    elif w["gen"] == "disk":
+        uv, vals = synth.disk(n, N, seed=seed, outlier_frac=0.01, vals_dtype=vdt)
+    else:
+        uv, vals = synth.uniform(n, S, N - S, seed=seed, vals_dtype=vdt)
+    if w.get("presort"):
+        # the data format of the workload: grouped into 32x32 uv tiles; the
+        # gridder still bins on the device at its own tile size
+        perm = synth.tile_sort(uv, N, 32)
+        uv, vals = np.ascontiguousarray(uv[perm]), np.ascontiguousarray(vals[perm])
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(vdt)
+    return uv, vals, gcf
+
+
+def single_options(w):
+    import gpugrid as gg
+    return gg.Options(
+        mode=gg.MODES[w["mode"]],
+        accum=gg.ACC_COMPENSATED if w["accum"] == "comp" else gg.ACC_PLAIN,
+        gcf_kind=gg.GCF_GAUSSIAN if w.get("gcf") == "gauss" else gg.GCF_TABLE,
+        layout=gg.LAYOUT_INTERLEAVED)
+
+
+def run_single(args, rank, world, local_rank, dist):
     import torch
     import gpugrid as gg
     import oracle as O
@@ -215,8 +687,8 @@ def run_ours(args, rank, world, local_rank, dist):
     dev = torch.device("cuda", local_rank)
     w = WORKLOADS[args.workload]
     N, S, n = w["N"], w["S"], w["npts"]
-    uv, vals, gcf = make_inputs(w, seed=1000 + rank)
-    o = options(w)
+    uv, vals, gcf = make_single(w, seed=1000 + rank)
+    o = single_options(w)
     odt = torch.complex64 if w["out"] == "c64" else torch.complex128
     d_uv = torch.from_numpy(uv).to(dev)
     d_vals = torch.from_numpy(vals).to(dev)
@@ -226,31 +698,23 @@ def run_ours(args, rank, world, local_rank, dist):
     ctx = gg.Context(local_rank)
     ctx.profile(True)
     stream = torch.cuda.current_stream(dev)
-
     for _ in range(args.warmup):
         ctx.grid(o, out, d_uv, d_vals, d_gcf, N, S)
     torch.cuda.synchronize()
     flags = ctx.read_flags()
-
-    # accuracy of this exact output against the FP64 oracle (rank 0)
     err = None
     if rank == 0 and not args.no_check:
-        pairs = lambda c: np.stack([c.real, c.imag], -1).astype(np.float64).reshape(-1, 2)
         nchk = n if N <= 4096 else n // 16
         if nchk < n:
             ctx.grid(o, out, d_uv[:nchk], d_vals[:nchk], d_gcf, N, S)
-        ref = O.grid_pz(uv[:nchk], pairs(vals[:nchk]), pairs(gcf.reshape(-1)), N, S,
-                        nthreads=os.cpu_count())
+        ref = O.grid_pz(uv[:nchk], pairs(vals[:nchk]), pairs(gcf), N, S, nthreads=os.cpu_count())
         got = torch.view_as_real(out).reshape(N, N, 2).cpu().numpy().astype(np.float64)
-        d = np.abs(got[..., 0] - ref[0, 0]).max(), np.abs(got[..., 1] - ref[1, 0]).max()
+        d = max(np.abs(got[..., 0] - ref[0, 0]).max(), np.abs(got[..., 1] - ref[1, 0]).max())
         den = max(np.abs(ref).max(), 1e-300)
         rms = np.sqrt(((got[..., 0] - ref[0, 0]) ** 2 + (got[..., 1] - ref[1, 0]) ** 2).sum()
                       / (ref ** 2).sum())
-        err = {"max_rel": float(max(d) / den), "rms_rel": float(rms),
-               "visibilities_checked": int(nchk)}
+        err = {"max_rel": float(d / den), "rms_rel": float(rms), "visibilities_checked": int(nchk)}
         del ref, got
-
-    # timed region
     start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     kern_ms, bin_ms = [], []
@@ -269,23 +733,17 @@ def run_ours(args, rank, world, local_rank, dist):
             bin_ms.append(b)
         torch.cuda.synchronize()
     launches = gg.kernel_launches() - l0
-    step_ms = [s.elapsed_time(e) for s, e in zip(start, end)]
-    total_ms = sum(step_ms)
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(start, end))
     if dist:
         t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-        dist.barrier()
-
-    # e2e through the C ABI from pinned host buffers
     e2e = None
     if not args.no_e2e:
         pin_uv = torch.from_numpy(uv.view(np.complex128).reshape(-1)).pin_memory().numpy()
         pin_vals = torch.from_numpy(vals).pin_memory().numpy()
         pin_gcf = torch.from_numpy(gcf.reshape(-1)).pin_memory().numpy()
-        pdt = np.complex64 if w["out"] == "c64" else np.complex128
         pin_out = torch.zeros(gg.padded_size(N, S), dtype=odt).pin_memory().numpy()
-        assert pin_out.dtype == pdt
         for _ in range(max(1, args.warmup)):
             gg.grid_host(o, pin_out, pin_uv, pin_vals, n, N, pin_gcf, S)
         ts = []
@@ -300,25 +758,16 @@ def run_ours(args, rank, world, local_rank, dist):
             t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e2e_s = float(t.item())
-        h2d = pin_uv.nbytes + pin_vals.nbytes + pin_gcf.nbytes
-        d2h = N * N * np.dtype(pdt).itemsize
         e2e = {"value": round(world * n * args.steps / e2e_s / 1e6, 3), "unit": "Mvis/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "h2d_bytes_per_step": int(pin_uv.nbytes + pin_vals.nbytes + pin_gcf.nbytes),
+               "d2h_bytes_per_step": int(N * N * pin_out.itemsize),
                "ms_per_step": round(1e3 * e2e_s / args.steps, 4),
                "api": "gg_grid_host (C ABI, pinned host buffers)"}
-
     if rank != 0:
         return None
-
     value = world * n * args.steps / (total_ms / 1e3) / 1e6
-    hbm, hbm_kind = peaks()
     vb = 8 if w["vals"] == "c64" else 16
     ob = 8 if w["out"] == "c64" else 16
-    mean_kern = statistics.mean(kern_ms)
-    # gridding-kernel algorithmic bytes per launch: staged records (8-byte
-    # packed index + value) + one read and one write of the grid by the
-    # flush reductions (window), the plain stores (gather), or the per-tap
-    # reductions' footprint (scatter: inputs 16 B uv + value per visibility)
     mode_name = {0: "scatter", 1: "gather", 2: "window", 3: "window"}[o.mode]
     if mode_name == "scatter":
         alg = n * (16 + vb) + 2 * N * N * ob
@@ -326,36 +775,29 @@ def run_ours(args, rank, world, local_rank, dist):
         alg = n * (8 + vb) + N * N * ob
     else:
         alg = n * (8 + vb) + 2 * N * N * ob
-    achieved = alg / (mean_kern / 1e3) / 1e9
-    tag = f"{mode_name}_{args.workload}"
-    traffic = traffic_from_profile(tag)
-    cpu_v, cpu_n, cpu_dt, cpu_threads = cpu_grid_rate(w, uv, vals, gcf, budget_s=args.cpu_budget)
+    mean_kern = statistics.mean(kern_ms)
+    cv, cn, cs, ct = cpu_rate([(uv[:1 << 20], vals[:1 << 20], gcf, N, S)], args.cpu_budget)
     res = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mvis/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(total_ms / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32" if w["vals"] == "c64" else "f64",
-        "data": "synthetic (seeded generators, shapes of the workload)",
-        "config": {"workload": f"{args.workload}: {w['desc']}",
-                   "method": mode_name, "l2": "flushed before every timed step (256 MiB write)",
+        "data": "synthetic (seeded generators with the workload's shapes)",
+        "config": {"workload": f"{args.workload}: {w['desc']}", "method": mode_name,
+                   "l2": "flushed before every timed step (256 MiB write)",
                    "img_dim": N, "gcf_dim": S, "oversample": 8, "visibilities": n,
                    "parallelism": f"replicas x{world}"},
         "tap_updates_per_s": round(value * 1e6 * S * S, 1),
         "phase_ms": {"setup_and_binning": round(statistics.mean(bin_ms), 4),
                      "gridding_kernel": round(mean_kern, 4)},
         "accuracy": err, "flags": flags,
-        "roofline": {"bound": "hbm", "kernel": f"{mode_name}_kernel",
-                     "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "peak_kind": f"{hbm_kind} (copy)",
-                     "traffic": traffic, "algorithmic_bytes_per_launch": int(alg)},
-        "cpu_baseline": {"value": round(cpu_v, 4), "unit": "Mvis/s", "cores": cpu_threads,
-                         "kind": "port",
-                         "sample": f"first {cpu_n} of {n} visibilities of the same "
-                                   f"workload, gridCPU_pz restatement over "
-                                   f"{cpu_threads} row bands ({cpu_dt:.1f} s)"},
-        "e2e": e2e,
-        "gpu_launches": int(launches),
+        "roofline": roofline(f"{mode_name}_kernel", alg, mean_kern,
+                             f"{mode_name}_{args.workload}"),
+        "cpu_baseline": {"value": round(cv, 4), "unit": "Mvis/s", "cores": ct, "kind": "port",
+                         "sample": f"first {cn} visibilities of the workload ({cs:.1f} s), "
+                                   f"gridCPU_pz restatement over {ct} row bands"},
+        "e2e": e2e, "gpu_launches": int(launches),
     }
     clocks = clk.summary()
     if clocks:
@@ -369,38 +811,65 @@ def run_ours(args, rank, world, local_rank, dist):
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    w = WORKLOADS[args.workload]
-    uv, vals, gcf = make_inputs(w, seed=1000)
-    threads = os.cpu_count() or 1
-    # size a step to ~budget seconds
-    rate, n_s, _, _ = cpu_grid_rate(w, uv, vals, gcf, budget_s=1.0, threads=threads)
-    n_step = int(min(len(uv), max(1 << 12, rate * 1e6 * args.cpu_budget / max(args.steps, 1))))
     import oracle as O
-    pairs = lambda c: np.stack([c.real, c.imag], -1).astype(np.float64).reshape(-1, 2)
-    g = pairs(gcf.reshape(-1))
-    pv = pairs(vals[:n_step])
+    w = WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    if w["kind"] == "single":
+        uv, vals, gcf = make_single(w, seed=1000)
+        jobs = [(uv, vals, gcf, w["N"], w["S"])]
+        desc_n = w["npts"]
+    else:
+        pools, specs, gcfs = stream_inputs(w["n"], seed=7)
+        jobs = []
+        for i in range(w["n"]):
+            uv, vals = slice_of(pools, specs, i)
+            jobs.append((uv, vals, gcfs[int(specs["S"][i])], int(specs["side"][i]),
+                         int(specs["S"][i])))
+        desc_n = int(specs["nvis"].sum())
+    # a step grids whole jobs (or a prefix of a single job) for about
+    # cpu_budget / steps seconds
+    per_step = max(0.5, args.cpu_budget / max(1, args.steps))
+
+    def step():
+        vis, t0 = 0, time.perf_counter()
+        for uv, vals, gcf, N, S in jobs:
+            if w["kind"] == "single":
+                # prefix sized to the budget (measured on the first step)
+                m = min(len(uv), step.prefix)
+                O.grid_pz(uv[:m], pairs(vals[:m]), pairs(gcf), N, S, nthreads=threads)
+                vis += m
+            else:
+                O.grid_pz(uv, pairs(vals), pairs(gcf), N, S, nthreads=threads)
+                vis += len(uv)
+            if time.perf_counter() - t0 >= per_step:
+                break
+        return vis, time.perf_counter() - t0
+    step.prefix = 1 << 16
+    if w["kind"] == "single":
+        v, dt = step()
+        step.prefix = int(min(len(jobs[0][0]), max(1 << 12, v * per_step / max(dt, 1e-6))))
     for _ in range(args.warmup):
-        O.grid_pz(uv[:n_step], pv, g, w["N"], w["S"], nthreads=threads)
-    t0 = time.perf_counter()
+        step()
+    tot_v, tot_t = 0, 0.0
     for _ in range(args.steps):
-        O.grid_pz(uv[:n_step], pv, g, w["N"], w["S"], nthreads=threads)
-    dt = time.perf_counter() - t0
-    v = n_step * args.steps / dt / 1e6
+        v, dt = step()
+        tot_v += v
+        tot_t += dt
+    val = tot_v / tot_t / 1e6
     return {
-        "metric": METRIC, "value": round(v, 4), "unit": "Mvis/s", "impl": "reference",
+        "metric": METRIC, "value": round(val, 4), "unit": "Mvis/s", "impl": "reference",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded generators, shapes of the workload)",
-        "config": {"workload": f"{args.workload}: {w['desc']}", "img_dim": w["N"],
-                   "gcf_dim": w["S"], "oversample": 8, "visibilities": w["npts"]},
-        "cpu_baseline": {"value": round(v, 4), "unit": "Mvis/s", "cores": threads,
+        "ms_per_step": round(1e3 * tot_t / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generators with the workload's shapes)",
+        "config": {"workload": f"{args.workload}: {w['desc']}", "visibilities_per_pass": desc_n},
+        "cpu_baseline": {"value": round(val, 4), "unit": "Mvis/s", "cores": threads,
                          "kind": "port",
-                         "sample": f"first {n_step} of {w['npts']} visibilities per step; "
-                                   f"gridCPU_pz restatement (oracle/grid_oracle.c) over "
-                                   f"{threads} row bands, bit-identical to the "
-                                   f"single-threaded reference"},
-        "e2e": {"value": round(v, 4), "unit": "Mvis/s", "h2d_bytes_per_step": 0,
+                         "sample": f"{tot_v // max(1, args.steps)} visibilities per step (a bounded "
+                                   f"prefix of the workload); gridCPU_pz restatement "
+                                   f"(oracle/grid_oracle.c) over {threads} row bands, "
+                                   f"bit-identical to the single-threaded reference"},
+        "e2e": {"value": round(val, 4), "unit": "Mvis/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
 
@@ -408,9 +877,9 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="tracks4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=8.0,
                     help="seconds of CPU gridding for the CPU baseline")
@@ -420,7 +889,6 @@ def main():
     if args.warmup < 3:
         log("bench: warm-up below 3 steps; using 3")
         args.warmup = 3
-
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
@@ -434,7 +902,9 @@ def main():
             torch.cuda.set_device(local_rank)
             td.init_process_group("nccl")
             dist = td
-        res = run_ours(args, rank, world, local_rank, dist)
+        kind = WORKLOADS[args.workload]["kind"]
+        fn = {"served": run_served, "batch": run_batch, "single": run_single}[kind]
+        res = fn(args, rank, world, local_rank, dist)
         if dist:
             dist.destroy_process_group()
     if res is not None and rank == 0:

@@ -161,6 +161,21 @@ int gg_grid_device(gg_context *ctx, const gg_options *opt, const gg_job *job,
 int gg_grid_batch(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
                   int32_t njobs, void *stream);
 
+/* ---- plans: a batch fixed once, launched many times ---------------------
+ * gg_plan_create validates the jobs, allocates the plan's own workspace and
+ * uploads its device tables (synchronously).  gg_plan_launch then only
+ * enqueues memsets and kernels on `stream` -- no host copies, allocations
+ * or synchronisation -- so it can be captured into a CUDA graph and
+ * replayed; every launch re-reads the jobs' input buffers and overwrites
+ * their outputs. */
+typedef struct gg_plan gg_plan;
+int gg_plan_create(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
+                   int32_t njobs, gg_plan **plan);
+int gg_plan_launch(gg_plan *plan, void *stream);
+/* the plan's flag counters, like gg_read_flags (synchronises the stream) */
+int gg_plan_read_flags(gg_plan *plan, void *stream, int32_t flags[4]);
+int gg_plan_destroy(gg_plan *plan);
+
 /* Counters of the last completed calls on this context (synchronises the
  * stream): [0] visibilities dropped because their oversample index fell
  * outside [0,G) (u not float-representable right below an integer),
@@ -195,6 +210,85 @@ int gg_vis2ints(int uv_type, const void *uv, int64_t npts, int32_t oversample,
 int gg_bin(gg_context *ctx, const gg_options *opt, int uv_type, const void *uv,
            int64_t npts, int64_t img_dim, int64_t gcf_dim, int32_t *bookmarks,
            int32_t *order, void *stream);
+
+/* ---- serving: continuous batching of gridding requests -----------------
+ * A server owns `streams` batch slots (each a context with its own workspace
+ * and CUDA stream) and a scheduler thread.  Requests are admitted in arrival
+ * order while the HBM budget allows (grid + staged inputs + workspace share);
+ * whenever a slot is free, every admitted request not yet started is
+ * gridded in one batched launch there, so requests that arrive while others
+ * are on the GPU overlap with them on the device.  Latency = arrival to
+ * grid ready on the host side of the stream. */
+typedef struct gg_server gg_server;
+
+#define GG_REQ_INPUTS_ON_DEVICE 1 /* uv / vals are device pointers            */
+#define GG_REQ_OUT_ON_DEVICE 2    /* out is a caller-owned device grid         */
+#define GG_REQ_KEEP_RESIDENT 4    /* out unused: the grid stays on the device,
+                                     owned by the server until release       */
+
+typedef struct gg_server_config {
+  int32_t device;
+  int32_t streams;          /* batch slots in flight (default 2)            */
+  int32_t max_batch_jobs;   /* per launch (default 256)                     */
+  int32_t reserved0;
+  int64_t max_batch_vis;    /* per launch (default 2^26)                    */
+  int64_t hbm_budget_bytes; /* admission budget (default 150e9)             */
+  gg_options options;       /* method, accumulation, ... of every request   */
+  int64_t reserved[4];
+} gg_server_config;
+
+typedef struct gg_request {
+  const void *uv;     /* host, or device with GG_REQ_INPUTS_ON_DEVICE        */
+  const void *vals;
+  void *out;          /* host grid (copied back), or a device grid with
+                         GG_REQ_OUT_ON_DEVICE; layout as gg_grid_device     */
+  int64_t npts, img_dim, gcf_dim;
+  int32_t uv_type, vals_type, out_type;
+  int32_t gcf_id;     /* table from gg_server_add_gcf; -1: options' GCF     */
+  int32_t flags;      /* GG_REQ_*                                            */
+  int32_t reserved0;
+  int64_t reserved[3];
+} gg_request;
+
+typedef struct gg_result {
+  int32_t status;     /* GG_OK or GG_ERR_*                                  */
+  int32_t reserved0;
+  double latency_s;   /* arrival -> grid ready                              */
+  double queue_s;     /* arrival -> launch                                  */
+  void *device_out;   /* GG_REQ_KEEP_RESIDENT: the grid on the device       */
+} gg_result;
+
+typedef struct gg_server_stats {
+  int64_t submitted, completed, failed, rejected, cancelled, batches;
+  int64_t visibilities;      /* gridded by completed requests               */
+  double span_s;             /* first arrival to last completion            */
+  double p50_latency_s, p99_latency_s, mean_latency_s, mean_batch_jobs;
+  int64_t hbm_in_use, hbm_peak;
+} gg_server_stats;
+
+int gg_server_default_config(gg_server_config *cfg);
+int gg_server_create(gg_server **srv, const gg_server_config *cfg);
+/* upload a GCF table once; requests refer to it by id */
+int gg_server_add_gcf(gg_server *srv, const void *host_table, int32_t vals_type,
+                      int64_t gcf_dim, int32_t *gcf_id);
+/* non-blocking; GG_ERR_BUDGET if the request alone exceeds the budget */
+int gg_server_submit(gg_server *srv, const gg_request *req, int64_t *ticket);
+/* submits request i at (now + offsets_s[i]) from a server-side thread
+ * (arrival traces, e.g. Poisson); tickets are assigned immediately */
+int gg_server_submit_schedule(gg_server *srv, const gg_request *reqs,
+                              const double *offsets_s, int64_t n,
+                              int64_t *tickets);
+/* GG_ERR_TIMEOUT when not complete within timeout_s (< 0: no limit) */
+int gg_server_wait(gg_server *srv, int64_t ticket, double timeout_s,
+                   gg_result *res);
+/* forget a completed ticket, freeing its resident grid */
+int gg_server_release(gg_server *srv, int64_t ticket);
+/* cancel a request that has not been launched yet */
+int gg_server_cancel(gg_server *srv, int64_t ticket);
+int gg_server_get_stats(gg_server *srv, gg_server_stats *st, int reset);
+/* wait until nothing is pending or in flight */
+int gg_server_drain(gg_server *srv, double timeout_s);
+int gg_server_destroy(gg_server *srv);
 
 /* ---- allocation-free moving window -------------------------------------
  * No counterpart in the reference.  Grids one job like gg_grid_device with

@@ -25,7 +25,7 @@ LIB = os.path.join(HERE, "libgg.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["gg_api.cu", "gg_bin.cu", "gg_scatter.cu", "gg_window.cu",
-           "gg_gather.cu", "gg_noalloc.cu"]
+           "gg_gather.cu", "gg_noalloc.cu", "gg_server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -197,6 +197,7 @@ struct Plan {
       o_count_vals, o_count_gcf, ws_bytes;
   int64_t vstride = 0, class_cap = 0;
   size_t table_bytes = 0;  // bytes uploaded from staging (jobs..class)
+  char *ws = nullptr;      // workspace the addresses are bound to
 };
 
 struct gg_context {
@@ -490,11 +491,9 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
   return GG_OK;
 }
 
-// Fix device addresses once the workspace exists; write tables to staging.
-static int plan_bind(gg_context *c, const gg_options *opt, Plan &pl) {
-  int st = c->ws.ensure(pl.ws_bytes);
-  if (st) return st;
-  char *ws = (char *)c->ws.p;
+// Fix device addresses for a workspace at `ws`; write the device tables
+// (jobs, bin jobs, bases, classes) into `host` (pl.table_bytes bytes).
+static void plan_bind(const gg_options *opt, Plan &pl, char *ws, char *host) {
   const bool binned = pl.mode != GG_MODE_SCATTER;
   const size_t vbytes = pl.vals_f64 ? 16 : 8;
   for (int k = 0; k < pl.njobs; ++k) {
@@ -516,28 +515,35 @@ static int plan_bind(gg_context *c, const gg_options *opt, Plan &pl) {
   // count-mode fills: resolve to absolute addresses
   for (auto &f : pl.count_fill)
     f.first = ws + pl.o_count_vals + vbytes * (size_t)reinterpret_cast<intptr_t>(f.first);
-  // pinned staging: wait until the previous upload has been consumed
-  GG_CUDA(cudaEventSynchronize(c->upload_done));
-  st = c->staging.ensure(pl.table_bytes);
-  if (st) return st;
-  char *h = (char *)c->staging.p;
-  memcpy(h + pl.o_jobs, pl.hjobs.data(), sizeof(JobDesc) * pl.njobs);
-  memcpy(h + pl.o_bin, pl.hbin.data(), sizeof(BinJob) * pl.njobs);
-  memcpy(h + pl.o_visb, pl.hvis_base.data(), sizeof(int64_t) * (pl.njobs + 1));
-  memcpy(h + pl.o_tileb, pl.htile_base.data(), sizeof(int) * (pl.njobs + 1));
-  memcpy(h + pl.o_class, pl.hclass.data(), sizeof(int) * pl.njobs);
-  return GG_OK;
+  memcpy(host + pl.o_jobs, pl.hjobs.data(), sizeof(JobDesc) * pl.njobs);
+  memcpy(host + pl.o_bin, pl.hbin.data(), sizeof(BinJob) * pl.njobs);
+  memcpy(host + pl.o_visb, pl.hvis_base.data(), sizeof(int64_t) * (pl.njobs + 1));
+  memcpy(host + pl.o_tileb, pl.htile_base.data(), sizeof(int) * (pl.njobs + 1));
+  memcpy(host + pl.o_class, pl.hclass.data(), sizeof(int) * pl.njobs);
+  pl.ws = ws;
 }
 
-// Enqueue the whole computation on stream s.
-static int plan_execute(gg_context *c, const gg_options *opt, Plan &pl,
-                        cudaStream_t s) {
-  char *ws = (char *)c->ws.p;
-  int *flags = (int *)c->flags.p;
-  GG_CUDA(cudaStreamWaitEvent(s, c->exec_done, 0));
-  if (c->profile) GG_CUDA(cudaEventRecord(c->prof[0], s));
-  GG_CUDA(cudaMemcpyAsync(ws, c->staging.p, pl.table_bytes, cudaMemcpyHostToDevice, s));
-  GG_CUDA(cudaEventRecord(c->upload_done, s));
+// Profiling events of one enqueue (null: none)
+struct ProfEvents {
+  cudaEvent_t ev[4];
+};
+
+// Enqueue the whole computation on stream s: zeroing, binning, work queue,
+// gridding kernels.  `upload` (pinned host tables) is copied into the
+// workspace first when given, and `upload_ev` recorded right after that copy
+// (the staging buffer is free again from there on, so the host can prepare
+// the next call while this one runs); a plan whose tables are already
+// resident passes null, and then nothing here reads host memory, allocates
+// or synchronises -- the sequence can be captured into a CUDA graph.
+static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int sm_count,
+                        cudaStream_t s, const void *upload, cudaEvent_t upload_ev,
+                        const ProfEvents *prof) {
+  char *ws = pl.ws;
+  if (prof) GG_CUDA(cudaEventRecord(prof->ev[0], s));
+  if (upload) {
+    GG_CUDA(cudaMemcpyAsync(ws, upload, pl.table_bytes, cudaMemcpyHostToDevice, s));
+    if (upload_ev) GG_CUDA(cudaEventRecord(upload_ev, s));
+  }
   const JobDesc *djobs = (const JobDesc *)(ws + pl.o_jobs);
   const int64_t *dvisb = (const int64_t *)(ws + pl.o_visb);
   const int *dtileb = (const int *)(ws + pl.o_tileb);
@@ -570,7 +576,7 @@ static int plan_execute(gg_context *c, const gg_options *opt, Plan &pl,
   g.group_warps = pl.group_warps;
   g.P = pl.P;
   g.flags = flags;
-  g.sm_count = c->sm_count;
+  g.sm_count = sm_count;
 
   if (pl.mode != GG_MODE_SCATTER) {
     BinBuffers b{};
@@ -602,7 +608,7 @@ static int plan_execute(gg_context *c, const gg_options *opt, Plan &pl,
     WorkItem *items = (WorkItem *)(ws + pl.o_items);
     GG_CUDA(launch_make_items((const int *)(ws + pl.o_bm), dtileb, dclass, pl.njobs,
                               pl.total_tiles, pl.chunk, items, pl.class_cap, flags + 8, s));
-    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[1], s));
+    if (prof) GG_CUDA(cudaEventRecord(prof->ev[1], s));
     for (size_t ci = 0; ci < pl.classes.size(); ++ci) {
       const auto &cl = pl.classes[ci];
       g.jobs = djobs;
@@ -614,9 +620,9 @@ static int plan_execute(gg_context *c, const gg_options *opt, Plan &pl,
       g.max_items = pl.class_cap;
       GG_CUDA(launch_window(g, s));
     }
-    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[2], s));
+    if (prof) GG_CUDA(cudaEventRecord(prof->ev[2], s));
   } else if (pl.mode == GG_MODE_GATHER) {
-    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[1], s));
+    if (prof) GG_CUDA(cudaEventRecord(prof->ev[1], s));
     for (const auto &cl : pl.classes) {
       g.jobs = djobs + cl.j0;
       g.njobs = cl.j1 - cl.j0;
@@ -625,9 +631,9 @@ static int plan_execute(gg_context *c, const gg_options *opt, Plan &pl,
       g.total_tiles = cl.t1 - cl.t0;
       GG_CUDA(launch_gather(g, s));
     }
-    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[2], s));
+    if (prof) GG_CUDA(cudaEventRecord(prof->ev[2], s));
   } else {
-    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[1], s));
+    if (prof) GG_CUDA(cudaEventRecord(prof->ev[1], s));
     for (const auto &cl : pl.classes) {
       g.jobs = djobs + cl.j0;
       g.njobs = cl.j1 - cl.j0;
@@ -636,7 +642,7 @@ static int plan_execute(gg_context *c, const gg_options *opt, Plan &pl,
       g.total_vis = cl.v1 - cl.v0;
       GG_CUDA(launch_scatter(g, s));
     }
-    if (c->profile) GG_CUDA(cudaEventRecord(c->prof[2], s));
+    if (prof) GG_CUDA(cudaEventRecord(prof->ev[2], s));
     if (pl.comp_lo) {
       for (int k = 0; k < pl.njobs; ++k) {
         const JobDesc &D = pl.hjobs[k];
@@ -645,11 +651,7 @@ static int plan_execute(gg_context *c, const gg_options *opt, Plan &pl,
       }
     }
   }
-  if (c->profile) {
-    GG_CUDA(cudaEventRecord(c->prof[3], s));
-    c->prof_recorded = 1;
-  }
-  GG_CUDA(cudaEventRecord(c->exec_done, s));
+  if (prof) GG_CUDA(cudaEventRecord(prof->ev[3], s));
   return GG_OK;
 }
 
@@ -661,9 +663,20 @@ static int grid_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs,
   if (st) return st;
   // the workspace may be reallocated: earlier work on it must be finished
   if (pl.ws_bytes > c->ws.n) GG_CUDA(cudaEventSynchronize(c->exec_done));
-  st = plan_bind(c, opt, pl);
+  if ((st = c->ws.ensure(pl.ws_bytes))) return st;
+  // pinned staging: the previous upload must have been consumed
+  GG_CUDA(cudaEventSynchronize(c->upload_done));
+  if ((st = c->staging.ensure(pl.table_bytes))) return st;
+  plan_bind(opt, pl, (char *)c->ws.p, (char *)c->staging.p);
+  GG_CUDA(cudaStreamWaitEvent(s, c->exec_done, 0));
+  ProfEvents pe;
+  for (int i = 0; i < 4; ++i) pe.ev[i] = c->prof[i];
+  st = plan_enqueue(opt, pl, (int *)c->flags.p, c->sm_count, s, c->staging.p,
+                    c->upload_done, c->profile ? &pe : nullptr);
   if (st) return st;
-  return plan_execute(c, opt, pl, s);
+  if (c->profile) c->prof_recorded = 1;
+  GG_CUDA(cudaEventRecord(c->exec_done, s));
+  return GG_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -777,6 +790,77 @@ int gg_read_flags(gg_context *ctx, void *stream, int32_t flags[4]) {
   return GG_OK;
 }
 
+}  // extern "C"
+
+struct gg_plan {
+  gg_context *ctx = nullptr;
+  gg_options opt;
+  Plan pl;
+  DevBuf ws, flags;
+};
+
+extern "C" {
+
+int gg_plan_create(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
+                   int32_t njobs, gg_plan **out) {
+  if (!ctx || !out) return fail(GG_ERR_ARG, "null argument");
+  *out = nullptr;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  GG_CUDA(cudaSetDevice(ctx->device));
+  std::unique_ptr<gg_plan> p(new (std::nothrow) gg_plan);
+  if (!p) return fail(GG_ERR_NOMEM, "plan allocation");
+  p->ctx = ctx;
+  p->opt = *opt;
+  int st = plan_build(ctx, opt, jobs, njobs, p->pl);
+  if (st) return st;
+  if ((st = p->ws.ensure(p->pl.ws_bytes))) return st;
+  if ((st = p->flags.ensure(64 * sizeof(int)))) {
+    p->ws.release();
+    return st;
+  }
+  std::vector<char> tables(p->pl.table_bytes);
+  plan_bind(opt, p->pl, (char *)p->ws.p, tables.data());
+  cudaError_t e = cudaMemcpy(p->ws.p, tables.data(), p->pl.table_bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(p->flags.p, 0, 64 * sizeof(int));
+  if (e != cudaSuccess) {
+    p->ws.release();
+    p->flags.release();
+    return cuda_fail(e, "plan upload");
+  }
+  *out = p.release();
+  return GG_OK;
+}
+
+int gg_plan_launch(gg_plan *p, void *stream) {
+  if (!p) return fail(GG_ERR_ARG, "plan: null");
+  GG_CUDA(cudaSetDevice(p->ctx->device));
+  return plan_enqueue(&p->opt, p->pl, (int *)p->flags.p, p->ctx->sm_count,
+                      (cudaStream_t)stream, nullptr, nullptr, nullptr);
+}
+
+int gg_plan_read_flags(gg_plan *p, void *stream, int32_t flags[4]) {
+  if (!p || !flags) return fail(GG_ERR_ARG, "null argument");
+  GG_CUDA(cudaSetDevice(p->ctx->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  int h[4];
+  GG_CUDA(cudaMemcpyAsync(h, p->flags.p, sizeof h, cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  GG_CUDA(cudaMemsetAsync(p->flags.p, 0, sizeof h, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < 4; ++i) flags[i] = h[i];
+  return GG_OK;
+}
+
+int gg_plan_destroy(gg_plan *p) {
+  if (!p) return GG_OK;
+  cudaSetDevice(p->ctx->device);
+  cudaDeviceSynchronize();
+  p->ws.release();
+  p->flags.release();
+  delete p;
+  return GG_OK;
+}
+
 int gg_profile_enable(gg_context *ctx, int on) {
   if (!ctx) return fail(GG_ERR_ARG, "ctx: null");
   std::lock_guard<std::mutex> lk(ctx->mu);
@@ -857,8 +941,10 @@ int gg_bin(gg_context *ctx, const gg_options *opt, int uv_type, const void *uv,
   if (pl.ws_bytes > ctx->ws.n) GG_CUDA(cudaEventSynchronize(ctx->exec_done));
   size_t order_off = align256(pl.ws_bytes);
   pl.ws_bytes = order_off + align256(sizeof(int) * (npts + 8));
-  st = plan_bind(ctx, &o, pl);
-  if (st) return st;
+  if ((st = ctx->ws.ensure(pl.ws_bytes))) return st;
+  GG_CUDA(cudaEventSynchronize(ctx->upload_done));
+  if ((st = ctx->staging.ensure(pl.table_bytes))) return st;
+  plan_bind(&o, pl, (char *)ctx->ws.p, (char *)ctx->staging.p);
   char *ws = (char *)ctx->ws.p;
   cudaStream_t s = (cudaStream_t)stream;
   GG_CUDA(cudaStreamWaitEvent(s, ctx->exec_done, 0));

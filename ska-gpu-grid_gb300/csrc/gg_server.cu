@@ -1,0 +1,612 @@
+// Request server: admission by HBM budget and continuous batching of
+// gridding requests over several CUDA streams (gg_server_* in gg.h).
+//
+// There is no counterpart in the reference, whose gridGPU serves one call at
+// a time on the default stream.  Design:
+//  * a scheduler thread owns `streams` slots; a slot = one gg_context (its
+//    own workspace) + one CUDA stream.  Whenever a slot is free and requests
+//    are pending, every pending request that fits the HBM budget (in arrival
+//    order, up to the batch limits) is staged and gridded there in ONE
+//    batched launch (gg_grid_batch: one binning pass and one persistent
+//    window kernel per support over all of them);
+//  * staging uses stream-ordered allocation (cudaMallocAsync from the
+//    device's memory pool) so that a batch allocates nothing synchronously;
+//    inputs and host-bound grids are freed in stream order after the copies;
+//  * completion is signalled by a host function enqueued behind the batch
+//    (cudaLaunchHostFunc), which only flags the slot and wakes the
+//    scheduler; the scheduler finishes the requests, returns their budget
+//    and wakes waiters;
+//  * latency is measured from a request's arrival (its submit time, or its
+//    scheduled time in a trace) to that completion.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "gg_internal.h"
+
+using gg::set_error;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+enum ReqState { R_SCHEDULED = 0, R_PENDING, R_LAUNCHED, R_DONE, R_FAILED, R_CANCELLED };
+
+struct Req {
+  int64_t ticket = 0;
+  gg_request r;
+  double t_arrival = 0, t_launch = 0, t_done = 0;
+  int state = R_SCHEDULED;
+  int status = GG_OK;
+  int64_t bytes = 0;          // budget charged while admitted
+  int64_t resident_bytes = 0; // part of `bytes` kept until release
+  void *d_uv = nullptr, *d_vals = nullptr, *d_out = nullptr;
+  bool own_uv = false, own_vals = false, own_out = false;
+  cudaStream_t stream = nullptr;
+};
+
+struct Slot {
+  cudaStream_t s = nullptr;
+  gg_context *ctx = nullptr;
+  std::vector<Req *> batch;
+  bool busy = false;
+  bool done = false;
+  struct gg_server *srv = nullptr;
+};
+
+int elem(int type) { return type == GG_C128 ? 16 : 8; }
+
+}  // namespace
+
+struct gg_server {
+  gg_server_config cfg;
+  Clock::time_point epoch;
+  std::mutex mu;
+  std::condition_variable cv_sched, cv_done, cv_feed;
+  std::deque<Req *> pending;
+  std::unordered_map<int64_t, std::unique_ptr<Req>> reqs;
+  int64_t next_ticket = 1;
+  int64_t used = 0, peak = 0;
+  bool stop = false;
+  std::vector<std::unique_ptr<Slot>> slots;
+  std::vector<void *> gcf_ptr;
+  std::vector<int64_t> gcf_dim;
+  std::vector<int> gcf_type;
+  std::thread sched;
+  std::vector<std::thread> feeders;
+  int feeders_running = 0;
+  // statistics
+  int64_t n_submitted = 0, n_completed = 0, n_failed = 0, n_rejected = 0,
+          n_cancelled = 0, n_batches = 0, n_batch_jobs = 0, n_vis = 0;
+  double first_arrival = -1, last_done = 0;
+  std::vector<double> lat;
+
+  double now() const {
+    return std::chrono::duration<double>(Clock::now() - epoch).count();
+  }
+};
+
+namespace {
+
+void on_batch_done(void *p) {
+  Slot *slot = static_cast<Slot *>(p);
+  gg_server *srv = slot->srv;
+  std::lock_guard<std::mutex> lk(srv->mu);
+  slot->done = true;
+  srv->cv_sched.notify_one();
+}
+
+// bytes a request holds on the device while admitted
+int64_t estimate(const gg_server *srv, const gg_request &r) {
+  const int64_t P = srv->cfg.options.polarizations;
+  const int64_t N = r.img_dim, n = r.npts;
+  const int64_t grid = (r.flags & GG_REQ_OUT_ON_DEVICE) ? 0 : elem(r.out_type) * P * N * N;
+  const int64_t inputs =
+      (r.flags & GG_REQ_INPUTS_ON_DEVICE) ? 0 : n * (elem(r.uv_type) + elem(r.vals_type) * P);
+  const int64_t tiles = ((N + 15) / 16) * ((N + 15) / 16);
+  const int64_t ws = n * (8 + 4 + 8 + 4 + elem(r.vals_type) * P) + tiles * 16;
+  return grid + inputs + ws + 4096;
+}
+
+int validate(const gg_server *srv, const gg_request &r) {
+  if (r.npts < 0 || (r.npts > 0 && (!r.uv || !r.vals)))
+    return set_error(GG_ERR_ARG, "server: request without inputs");
+  if (r.img_dim < 1 || r.img_dim > 32768) return set_error(GG_ERR_ARG, "server: img_dim");
+  if (r.gcf_dim != 4 && r.gcf_dim != 8 && r.gcf_dim != 16 && r.gcf_dim != 32)
+    return set_error(GG_ERR_ARG, "server: gcf_dim not in {4,8,16,32}");
+  if ((r.uv_type != GG_C64 && r.uv_type != GG_C128) ||
+      (r.vals_type != GG_C64 && r.vals_type != GG_C128) ||
+      (r.out_type != GG_C64 && r.out_type != GG_C128))
+    return set_error(GG_ERR_ARG, "server: element type");
+  if ((r.flags & GG_REQ_OUT_ON_DEVICE) && !r.out)
+    return set_error(GG_ERR_ARG, "server: GG_REQ_OUT_ON_DEVICE without out");
+  if (!(r.flags & (GG_REQ_OUT_ON_DEVICE | GG_REQ_KEEP_RESIDENT)) && !r.out)
+    return set_error(GG_ERR_ARG, "server: no output (host out, device out or keep resident)");
+  if (r.gcf_id >= 0) {
+    if (r.gcf_id >= (int)srv->gcf_ptr.size())
+      return set_error(GG_ERR_ARG, "server: unknown gcf_id");
+    if (srv->gcf_dim[r.gcf_id] != r.gcf_dim || srv->gcf_type[r.gcf_id] != r.vals_type)
+      return set_error(GG_ERR_ARG, "server: gcf_id does not match gcf_dim / vals_type");
+  } else if (srv->cfg.options.gcf_kind == GG_GCF_TABLE) {
+    return set_error(GG_ERR_ARG, "server: TABLE GCF needs a gcf_id");
+  }
+  return GG_OK;
+}
+
+void finish_batch(gg_server *srv, Slot *slot) {
+  const double t = srv->now();
+  for (Req *q : slot->batch) {
+    if (q->state == R_LAUNCHED && q->status == GG_OK) {
+      q->state = R_DONE;
+      q->t_done = t;
+      ++srv->n_completed;
+      srv->n_vis += q->r.npts;
+      srv->lat.push_back(t - q->t_arrival);
+    } else {
+      q->state = R_FAILED;
+      q->t_done = t;
+      q->resident_bytes = 0;  // a failed request keeps no grid
+      ++srv->n_failed;
+    }
+    srv->used -= q->bytes - q->resident_bytes;
+    q->bytes = q->resident_bytes;
+  }
+  srv->last_done = t;
+  slot->batch.clear();
+  slot->busy = false;
+  slot->done = false;
+  srv->cv_done.notify_all();
+}
+
+// Stage and launch one batch on a slot (called without the lock).
+void launch_batch(gg_server *srv, Slot *slot) {
+  cudaSetDevice(srv->cfg.device);
+  cudaStream_t s = slot->s;
+  std::vector<gg_job> jobs;
+  jobs.reserve(slot->batch.size());
+  int st = GG_OK;
+  const int64_t P = srv->cfg.options.polarizations;
+  for (Req *q : slot->batch) {
+    const gg_request &r = q->r;
+    q->stream = s;
+    cudaError_t e = cudaSuccess;
+    if (r.flags & GG_REQ_INPUTS_ON_DEVICE) {
+      q->d_uv = const_cast<void *>(r.uv);
+      q->d_vals = const_cast<void *>(r.vals);
+    } else if (r.npts > 0) {
+      const size_t bu = (size_t)r.npts * elem(r.uv_type);
+      const size_t bv = (size_t)r.npts * elem(r.vals_type) * P;
+      e = cudaMallocAsync(&q->d_uv, bu, s);
+      if (e == cudaSuccess) {
+        q->own_uv = true;
+        e = cudaMallocAsync(&q->d_vals, bv, s);
+      }
+      if (e == cudaSuccess) {
+        q->own_vals = true;
+        e = cudaMemcpyAsync(q->d_uv, r.uv, bu, cudaMemcpyHostToDevice, s);
+      }
+      if (e == cudaSuccess) e = cudaMemcpyAsync(q->d_vals, r.vals, bv, cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess) {
+      if (r.flags & GG_REQ_OUT_ON_DEVICE) {
+        q->d_out = r.out;
+      } else {
+        e = cudaMallocAsync(&q->d_out, (size_t)elem(r.out_type) * P * r.img_dim * r.img_dim, s);
+        if (e == cudaSuccess) q->own_out = true;
+      }
+    }
+    if (e != cudaSuccess) {
+      q->status = e == cudaErrorMemoryAllocation ? GG_ERR_NOMEM : GG_ERR_CUDA;
+      st = q->status;
+      break;
+    }
+    gg_job j;
+    memset(&j, 0, sizeof j);
+    j.out = q->d_out;
+    j.uv = q->d_uv;
+    j.vals = q->d_vals;
+    j.gcf = r.gcf_id >= 0 ? srv->gcf_ptr[r.gcf_id] : nullptr;
+    j.npts = r.npts;
+    j.img_dim = r.img_dim;
+    j.gcf_dim = r.gcf_dim;
+    j.uv_type = r.uv_type;
+    j.vals_type = r.vals_type;
+    j.out_type = r.out_type;
+    jobs.push_back(j);
+  }
+  if (st == GG_OK) st = gg_grid_batch(slot->ctx, &srv->cfg.options, jobs.data(),
+                                      (int32_t)jobs.size(), s);
+  for (Req *q : slot->batch) {
+    if (st != GG_OK && q->status == GG_OK) q->status = st;
+    const gg_request &r = q->r;
+    const bool host_out = !(r.flags & (GG_REQ_OUT_ON_DEVICE | GG_REQ_KEEP_RESIDENT));
+    if (st == GG_OK && host_out && q->d_out)
+      cudaMemcpyAsync(r.out, q->d_out, (size_t)elem(r.out_type) * P * r.img_dim * r.img_dim,
+                      cudaMemcpyDeviceToHost, s);
+    if (q->own_uv) cudaFreeAsync(q->d_uv, s);
+    if (q->own_vals) cudaFreeAsync(q->d_vals, s);
+    q->own_uv = q->own_vals = false;
+    q->d_uv = q->d_vals = nullptr;
+    if (q->own_out && (host_out || st != GG_OK)) {
+      cudaFreeAsync(q->d_out, s);
+      q->own_out = false;
+      q->d_out = nullptr;
+    }
+  }
+  if (cudaLaunchHostFunc(s, on_batch_done, slot) != cudaSuccess) {
+    // no callback: finish synchronously
+    cudaStreamSynchronize(s);
+    on_batch_done(slot);
+  }
+}
+
+void scheduler(gg_server *srv) {
+  cudaSetDevice(srv->cfg.device);
+  std::unique_lock<std::mutex> lk(srv->mu);
+  for (;;) {
+    for (auto &sl : srv->slots)
+      if (sl->busy && sl->done) finish_batch(srv, sl.get());
+    Slot *free_slot = nullptr;
+    for (auto &sl : srv->slots)
+      if (!sl->busy) {
+        free_slot = sl.get();
+        break;
+      }
+    if (free_slot && !srv->pending.empty()) {
+      // admit in arrival order while the budget and batch limits allow
+      int64_t vis = 0;
+      while (!srv->pending.empty() &&
+             (int)free_slot->batch.size() < srv->cfg.max_batch_jobs) {
+        Req *q = srv->pending.front();
+        const int64_t b = estimate(srv, q->r);
+        if (srv->used + b > srv->cfg.hbm_budget_bytes) break;
+        if (!free_slot->batch.empty() && vis + q->r.npts > srv->cfg.max_batch_vis) break;
+        srv->pending.pop_front();
+        q->bytes = b;
+        q->resident_bytes = (q->r.flags & GG_REQ_KEEP_RESIDENT)
+                                ? (int64_t)elem(q->r.out_type) * srv->cfg.options.polarizations *
+                                      q->r.img_dim * q->r.img_dim
+                                : 0;
+        srv->used += b;
+        srv->peak = std::max(srv->peak, srv->used);
+        q->state = R_LAUNCHED;
+        q->t_launch = srv->now();
+        vis += q->r.npts;
+        free_slot->batch.push_back(q);
+      }
+      if (!free_slot->batch.empty()) {
+        free_slot->busy = true;
+        free_slot->done = false;
+        ++srv->n_batches;
+        srv->n_batch_jobs += (int64_t)free_slot->batch.size();
+        lk.unlock();
+        launch_batch(srv, free_slot);
+        lk.lock();
+        continue;
+      }
+    }
+    bool any_busy = false;
+    for (auto &sl : srv->slots) any_busy |= sl->busy;
+    if (srv->stop && srv->pending.empty() && !any_busy && srv->feeders_running == 0) break;
+    srv->cv_sched.wait(lk);
+  }
+}
+
+void enqueue_locked(gg_server *srv, Req *q, double t_arrival) {
+  q->t_arrival = t_arrival;
+  q->state = R_PENDING;
+  if (srv->first_arrival < 0 || t_arrival < srv->first_arrival) srv->first_arrival = t_arrival;
+  srv->pending.push_back(q);
+  srv->cv_sched.notify_one();
+}
+
+}  // namespace
+
+extern "C" {
+
+int gg_server_default_config(gg_server_config *cfg) {
+  if (!cfg) return set_error(GG_ERR_ARG, "cfg: null");
+  memset(cfg, 0, sizeof *cfg);
+  cfg->device = 0;
+  cfg->streams = 2;
+  cfg->max_batch_jobs = 256;
+  cfg->max_batch_vis = 1ll << 26;
+  cfg->hbm_budget_bytes = 150000000000ll;
+  gg_default_options(&cfg->options);
+  cfg->options.mode = GG_MODE_WINDOW;
+  cfg->options.accum = GG_ACC_COMPENSATED;
+  cfg->options.layout = GG_LAYOUT_INTERLEAVED;
+  return GG_OK;
+}
+
+int gg_server_create(gg_server **out, const gg_server_config *cfg) {
+  if (!out || !cfg) return set_error(GG_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (cfg->streams < 1 || cfg->streams > 16) return set_error(GG_ERR_ARG, "streams 1..16");
+  if (cfg->max_batch_jobs < 1 || cfg->max_batch_vis < 1 || cfg->hbm_budget_bytes < 1)
+    return set_error(GG_ERR_ARG, "batch limits / budget must be positive");
+  std::unique_ptr<gg_server> srv(new (std::nothrow) gg_server);
+  if (!srv) return set_error(GG_ERR_NOMEM, "server allocation");
+  srv->cfg = *cfg;
+  srv->epoch = Clock::now();
+  if (cudaSetDevice(cfg->device) != cudaSuccess) return set_error(GG_ERR_CUDA, "cudaSetDevice");
+  // keep freed stream-ordered memory in the pool between batches
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, cfg->device) == cudaSuccess) {
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  for (int i = 0; i < cfg->streams; ++i) {
+    std::unique_ptr<Slot> sl(new Slot);
+    sl->srv = srv.get();
+    int st = gg_create(&sl->ctx, cfg->device);
+    if (st) {
+      for (auto &x : srv->slots) {
+        gg_destroy(x->ctx);
+        cudaStreamDestroy(x->s);
+      }
+      return st;
+    }
+    cudaStreamCreateWithFlags(&sl->s, cudaStreamNonBlocking);
+    srv->slots.push_back(std::move(sl));
+  }
+  gg_server *p = srv.release();
+  p->sched = std::thread(scheduler, p);
+  *out = p;
+  return GG_OK;
+}
+
+int gg_server_add_gcf(gg_server *srv, const void *host_table, int32_t vals_type,
+                      int64_t gcf_dim, int32_t *gcf_id) {
+  if (!srv || !host_table || !gcf_id) return set_error(GG_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  const int64_t G = srv->cfg.options.oversample;
+  const size_t bytes = (size_t)elem(vals_type) * G * G * gcf_dim * gcf_dim;
+  void *d = nullptr;
+  cudaSetDevice(srv->cfg.device);
+  if (cudaMalloc(&d, bytes) != cudaSuccess) return set_error(GG_ERR_NOMEM, "gcf table");
+  if (cudaMemcpy(d, host_table, bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(d);
+    return set_error(GG_ERR_CUDA, "gcf upload");
+  }
+  srv->gcf_ptr.push_back(d);
+  srv->gcf_dim.push_back(gcf_dim);
+  srv->gcf_type.push_back(vals_type);
+  *gcf_id = (int32_t)srv->gcf_ptr.size() - 1;
+  return GG_OK;
+}
+
+int gg_server_submit(gg_server *srv, const gg_request *req, int64_t *ticket) {
+  if (!srv || !req || !ticket) return set_error(GG_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  if (srv->stop) return set_error(GG_ERR_STATE, "server is shutting down");
+  int st = validate(srv, *req);
+  if (st) return st;
+  if (estimate(srv, *req) > srv->cfg.hbm_budget_bytes) {
+    ++srv->n_rejected;
+    return set_error(GG_ERR_BUDGET, "request larger than the server's HBM budget");
+  }
+  std::unique_ptr<Req> q(new Req);
+  q->ticket = srv->next_ticket++;
+  q->r = *req;
+  Req *raw = q.get();
+  srv->reqs[q->ticket] = std::move(q);
+  ++srv->n_submitted;
+  enqueue_locked(srv, raw, srv->now());
+  *ticket = raw->ticket;
+  return GG_OK;
+}
+
+int gg_server_submit_schedule(gg_server *srv, const gg_request *reqs,
+                              const double *offsets_s, int64_t n, int64_t *tickets) {
+  if (!srv || (n > 0 && (!reqs || !offsets_s || !tickets)))
+    return set_error(GG_ERR_ARG, "null argument");
+  std::vector<std::pair<double, Req *>> plan;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    if (srv->stop) return set_error(GG_ERR_STATE, "server is shutting down");
+    const double t0 = srv->now();
+    for (int64_t i = 0; i < n; ++i) {
+      std::unique_ptr<Req> q(new Req);
+      q->ticket = srv->next_ticket++;
+      q->r = reqs[i];
+      tickets[i] = q->ticket;
+      int st = validate(srv, reqs[i]);
+      if (!st && estimate(srv, reqs[i]) > srv->cfg.hbm_budget_bytes) {
+        st = GG_ERR_BUDGET;
+        ++srv->n_rejected;
+      }
+      ++srv->n_submitted;
+      if (st) {
+        q->state = R_FAILED;
+        q->status = st;
+        ++srv->n_failed;
+      } else {
+        plan.push_back({t0 + std::max(0.0, offsets_s[i]), q.get()});
+      }
+      srv->reqs[q->ticket] = std::move(q);
+    }
+    ++srv->feeders_running;
+  }
+  std::sort(plan.begin(), plan.end(),
+            [](const std::pair<double, Req *> &a, const std::pair<double, Req *> &b) {
+              return a.first < b.first;
+            });
+  srv->feeders.emplace_back([srv, plan]() {
+    for (const auto &e : plan) {
+      const auto when = srv->epoch + std::chrono::duration_cast<Clock::duration>(
+                                         std::chrono::duration<double>(e.first));
+      {
+        // sleep to within ~100 us of the arrival (woken early on shutdown),
+        // then spin for precision
+        std::unique_lock<std::mutex> lk(srv->mu);
+        srv->cv_feed.wait_until(lk, when - std::chrono::microseconds(100),
+                                [srv] { return srv->stop; });
+        if (srv->stop) break;
+      }
+      while (Clock::now() < when) {
+      }
+      std::lock_guard<std::mutex> lk(srv->mu);
+      if (e.second->state == R_SCHEDULED) enqueue_locked(srv, e.second, e.first);
+    }
+    std::lock_guard<std::mutex> lk(srv->mu);
+    --srv->feeders_running;
+    srv->cv_sched.notify_one();
+  });
+  return GG_OK;
+}
+
+int gg_server_wait(gg_server *srv, int64_t ticket, double timeout_s, gg_result *res) {
+  if (!srv) return set_error(GG_ERR_ARG, "server: null");
+  std::unique_lock<std::mutex> lk(srv->mu);
+  auto it = srv->reqs.find(ticket);
+  if (it == srv->reqs.end()) return set_error(GG_ERR_ARG, "unknown ticket");
+  Req *q = it->second.get();
+  auto finished = [q] { return q->state >= R_DONE; };
+  if (timeout_s < 0) {
+    srv->cv_done.wait(lk, finished);
+  } else if (!srv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), finished)) {
+    return set_error(GG_ERR_TIMEOUT, "request not complete within the timeout");
+  }
+  if (res) {
+    memset(res, 0, sizeof *res);
+    res->status = q->state == R_CANCELLED ? GG_ERR_CANCELLED : q->status;
+    res->latency_s = q->t_done - q->t_arrival;
+    res->queue_s = q->t_launch > 0 ? q->t_launch - q->t_arrival : 0.0;
+    res->device_out = (q->r.flags & GG_REQ_KEEP_RESIDENT) ? q->d_out : nullptr;
+  }
+  if (q->state == R_CANCELLED) return set_error(GG_ERR_CANCELLED, "request cancelled");
+  if (q->status != GG_OK) return set_error(q->status, "request failed");
+  return GG_OK;
+}
+
+int gg_server_release(gg_server *srv, int64_t ticket) {
+  if (!srv) return set_error(GG_ERR_ARG, "server: null");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  auto it = srv->reqs.find(ticket);
+  if (it == srv->reqs.end()) return set_error(GG_ERR_ARG, "unknown ticket");
+  Req *q = it->second.get();
+  if (q->state < R_DONE) return set_error(GG_ERR_STATE, "request still in progress");
+  if (q->own_out && q->d_out) {
+    cudaSetDevice(srv->cfg.device);
+    cudaFreeAsync(q->d_out, q->stream);
+  }
+  srv->used -= q->bytes;
+  srv->reqs.erase(it);
+  srv->cv_sched.notify_one();
+  return GG_OK;
+}
+
+int gg_server_cancel(gg_server *srv, int64_t ticket) {
+  if (!srv) return set_error(GG_ERR_ARG, "server: null");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  auto it = srv->reqs.find(ticket);
+  if (it == srv->reqs.end()) return set_error(GG_ERR_ARG, "unknown ticket");
+  Req *q = it->second.get();
+  if (q->state == R_PENDING) {
+    srv->pending.erase(std::find(srv->pending.begin(), srv->pending.end(), q));
+  } else if (q->state != R_SCHEDULED) {
+    return set_error(GG_ERR_STATE, "request already launched or finished");
+  }
+  q->state = R_CANCELLED;
+  q->t_done = srv->now();
+  ++srv->n_cancelled;
+  srv->cv_done.notify_all();
+  return GG_OK;
+}
+
+int gg_server_get_stats(gg_server *srv, gg_server_stats *st, int reset) {
+  if (!srv || !st) return set_error(GG_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(srv->mu);
+  memset(st, 0, sizeof *st);
+  st->submitted = srv->n_submitted;
+  st->completed = srv->n_completed;
+  st->failed = srv->n_failed;
+  st->rejected = srv->n_rejected;
+  st->cancelled = srv->n_cancelled;
+  st->batches = srv->n_batches;
+  st->visibilities = srv->n_vis;
+  st->span_s = srv->first_arrival >= 0 ? srv->last_done - srv->first_arrival : 0.0;
+  st->mean_batch_jobs = srv->n_batches ? (double)srv->n_batch_jobs / srv->n_batches : 0.0;
+  st->hbm_in_use = srv->used;
+  st->hbm_peak = srv->peak;
+  if (!srv->lat.empty()) {
+    std::vector<double> v(srv->lat);
+    auto pct = [&v](double q) {
+      size_t k = (size_t)std::min<double>(v.size() - 1, std::max(0.0, q * (v.size() - 1) + 0.5));
+      std::nth_element(v.begin(), v.begin() + k, v.end());
+      return v[k];
+    };
+    st->p50_latency_s = pct(0.50);
+    st->p99_latency_s = pct(0.99);
+    double sum = 0;
+    for (double x : srv->lat) sum += x;
+    st->mean_latency_s = sum / srv->lat.size();
+  }
+  if (reset) {
+    srv->n_submitted = srv->n_completed = srv->n_failed = srv->n_rejected = 0;
+    srv->n_cancelled = srv->n_batches = srv->n_batch_jobs = srv->n_vis = 0;
+    srv->first_arrival = -1;
+    srv->last_done = 0;
+    srv->lat.clear();
+    srv->peak = srv->used;
+  }
+  return GG_OK;
+}
+
+int gg_server_drain(gg_server *srv, double timeout_s) {
+  if (!srv) return set_error(GG_ERR_ARG, "server: null");
+  std::unique_lock<std::mutex> lk(srv->mu);
+  auto idle = [srv] {
+    if (!srv->pending.empty() || srv->feeders_running) return false;
+    for (auto &sl : srv->slots)
+      if (sl->busy) return false;
+    return true;
+  };
+  if (timeout_s < 0) {
+    srv->cv_done.wait(lk, idle);
+  } else if (!srv->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), idle)) {
+    return set_error(GG_ERR_TIMEOUT, "server still busy after the timeout");
+  }
+  return GG_OK;
+}
+
+int gg_server_destroy(gg_server *srv) {
+  if (!srv) return GG_OK;
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->stop = true;
+    // requests whose arrival time has not come are dropped
+    for (auto &kv : srv->reqs)
+      if (kv.second->state == R_SCHEDULED) kv.second->state = R_CANCELLED;
+    srv->cv_sched.notify_all();
+    srv->cv_feed.notify_all();
+  }
+  for (auto &t : srv->feeders) t.join();
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->cv_sched.notify_all();
+  }
+  srv->sched.join();
+  cudaSetDevice(srv->cfg.device);
+  for (auto &sl : srv->slots) cudaStreamSynchronize(sl->s);
+  for (auto &kv : srv->reqs)
+    if (kv.second->own_out && kv.second->d_out) cudaFree(kv.second->d_out);
+  cudaDeviceSynchronize();
+  for (auto &sl : srv->slots) {
+    gg_destroy(sl->ctx);
+    cudaStreamDestroy(sl->s);
+  }
+  for (void *p : srv->gcf_ptr) cudaFree(p);
+  delete srv;
+  return GG_OK;
+}
+
+}  // extern "C"

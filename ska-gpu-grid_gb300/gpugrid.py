@@ -68,6 +68,42 @@ class gg_job(ctypes.Structure):
                 ("reserved", ctypes.c_int64 * 4)]
 
 
+REQ_INPUTS_ON_DEVICE, REQ_OUT_ON_DEVICE, REQ_KEEP_RESIDENT = 1, 2, 4
+
+
+class gg_server_config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("streams", ctypes.c_int32),
+                ("max_batch_jobs", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+                ("max_batch_vis", ctypes.c_int64), ("hbm_budget_bytes", ctypes.c_int64),
+                ("options", gg_options), ("reserved", ctypes.c_int64 * 4)]
+
+
+class gg_request(ctypes.Structure):
+    _fields_ = [("uv", ctypes.c_void_p), ("vals", ctypes.c_void_p),
+                ("out", ctypes.c_void_p), ("npts", ctypes.c_int64),
+                ("img_dim", ctypes.c_int64), ("gcf_dim", ctypes.c_int64),
+                ("uv_type", ctypes.c_int32), ("vals_type", ctypes.c_int32),
+                ("out_type", ctypes.c_int32), ("gcf_id", ctypes.c_int32),
+                ("flags", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+                ("reserved", ctypes.c_int64 * 3)]
+
+
+class gg_result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+                ("latency_s", ctypes.c_double), ("queue_s", ctypes.c_double),
+                ("device_out", ctypes.c_void_p)]
+
+
+class gg_server_stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in
+                ("submitted", "completed", "failed", "rejected", "cancelled",
+                 "batches", "visibilities")] + \
+               [(n, ctypes.c_double) for n in
+                ("span_s", "p50_latency_s", "p99_latency_s", "mean_latency_s",
+                 "mean_batch_jobs")] + \
+               [("hbm_in_use", ctypes.c_int64), ("hbm_peak", ctypes.c_int64)]
+
+
 def _load():
     if not os.path.exists(LIB_PATH):
         raise ImportError(
@@ -100,6 +136,22 @@ def _load():
         "gg_vis2ints": ([ctypes.c_int, vp, i64, i32, vp, vp], ctypes.c_int),
         "gg_bin": ([vp, P(gg_options), ctypes.c_int, vp, i64, i64, i64, vp, vp,
                     vp], ctypes.c_int),
+        "gg_plan_create": ([vp, P(gg_options), P(gg_job), i32, P(vp)], ctypes.c_int),
+        "gg_plan_launch": ([vp, vp], ctypes.c_int),
+        "gg_plan_read_flags": ([vp, vp, P(i32)], ctypes.c_int),
+        "gg_plan_destroy": ([vp], ctypes.c_int),
+        "gg_server_default_config": ([P(gg_server_config)], ctypes.c_int),
+        "gg_server_create": ([P(vp), P(gg_server_config)], ctypes.c_int),
+        "gg_server_add_gcf": ([vp, vp, i32, i64, P(i32)], ctypes.c_int),
+        "gg_server_submit": ([vp, P(gg_request), P(i64)], ctypes.c_int),
+        "gg_server_submit_schedule": ([vp, P(gg_request), P(ctypes.c_double), i64,
+                                       P(i64)], ctypes.c_int),
+        "gg_server_wait": ([vp, i64, ctypes.c_double, P(gg_result)], ctypes.c_int),
+        "gg_server_release": ([vp, i64], ctypes.c_int),
+        "gg_server_cancel": ([vp, i64], ctypes.c_int),
+        "gg_server_get_stats": ([vp, P(gg_server_stats), ctypes.c_int], ctypes.c_int),
+        "gg_server_drain": ([vp, ctypes.c_double], ctypes.c_int),
+        "gg_server_destroy": ([vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -333,6 +385,127 @@ class Context:
                           npts, img_dim, gcf_dim, bm.data_ptr(), order.data_ptr(),
                           ctypes.c_void_p(s.cuda_stream)))
         return bm, order
+
+
+class Plan:
+    """A batch of jobs fixed once (gg_plan_create); launch() only enqueues
+    memsets and kernels, so it can be captured into a CUDA graph."""
+
+    def __init__(self, ctx: Context, opts: Options, jobs: list[gg_job]):
+        self._h = ctypes.c_void_p()
+        arr = (gg_job * len(jobs))(*jobs)
+        _check(LIB.gg_plan_create(ctx._h, ctypes.byref(opts.c()), arr, len(jobs),
+                                  ctypes.byref(self._h)))
+        self.ctx = ctx
+
+    def launch(self, stream=None) -> None:
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream(self.ctx.device)
+        _check(LIB.gg_plan_launch(self._h, ctypes.c_void_p(s.cuda_stream)))
+
+    def read_flags(self, stream=None) -> list[int]:
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream(self.ctx.device)
+        f = (ctypes.c_int32 * 4)()
+        _check(LIB.gg_plan_read_flags(self._h, ctypes.c_void_p(s.cuda_stream), f))
+        return list(f)
+
+    def close(self) -> None:
+        if self._h:
+            LIB.gg_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """gg_server: admission by HBM budget and continuous batching."""
+
+    def __init__(self, device: int = 0, streams: int = 2, max_batch_jobs: int = 256,
+                 max_batch_vis: int = 1 << 26, hbm_budget: float = 150e9,
+                 options: Options | None = None):
+        cfg = gg_server_config()
+        _check(LIB.gg_server_default_config(ctypes.byref(cfg)))
+        cfg.device, cfg.streams = device, streams
+        cfg.max_batch_jobs, cfg.max_batch_vis = max_batch_jobs, max_batch_vis
+        cfg.hbm_budget_bytes = int(hbm_budget)
+        if options is not None:
+            cfg.options = options.c()
+        self._h = ctypes.c_void_p()
+        _check(LIB.gg_server_create(ctypes.byref(self._h), ctypes.byref(cfg)))
+
+    def add_gcf(self, table: np.ndarray) -> int:
+        t = np.ascontiguousarray(table)
+        gid = ctypes.c_int32()
+        vt = C128 if t.dtype == np.complex128 else C64
+        S = t.shape[-1]
+        _check(LIB.gg_server_add_gcf(self._h, t.ctypes.data, vt, S, ctypes.byref(gid)))
+        return gid.value
+
+    @staticmethod
+    def request(uv_ptr, vals_ptr, out_ptr, npts, img_dim, gcf_dim, gcf_id=-1,
+                flags=0, uv_type=C128, vals_type=C64, out_type=C64) -> gg_request:
+        r = gg_request()
+        r.uv, r.vals, r.out = uv_ptr, vals_ptr, out_ptr
+        r.npts, r.img_dim, r.gcf_dim = npts, img_dim, gcf_dim
+        r.uv_type, r.vals_type, r.out_type = uv_type, vals_type, out_type
+        r.gcf_id, r.flags = gcf_id, flags
+        return r
+
+    def submit(self, req: gg_request) -> int:
+        t = ctypes.c_int64()
+        _check(LIB.gg_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)))
+        return t.value
+
+    def submit_schedule(self, reqs: list[gg_request], offsets_s) -> np.ndarray:
+        n = len(reqs)
+        arr = (gg_request * n)(*reqs)
+        off = np.ascontiguousarray(offsets_s, np.float64)
+        tickets = np.zeros(n, np.int64)
+        _check(LIB.gg_server_submit_schedule(
+            self._h, arr, off.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n,
+            tickets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return tickets
+
+    def wait(self, ticket: int, timeout: float = -1.0) -> gg_result:
+        r = gg_result()
+        _check(LIB.gg_server_wait(self._h, ticket, timeout, ctypes.byref(r)))
+        return r
+
+    def release(self, ticket: int) -> None:
+        _check(LIB.gg_server_release(self._h, ticket))
+
+    def cancel(self, ticket: int) -> None:
+        _check(LIB.gg_server_cancel(self._h, ticket))
+
+    def stats(self, reset: bool = False) -> dict:
+        s = gg_server_stats()
+        _check(LIB.gg_server_get_stats(self._h, ctypes.byref(s), int(reset)))
+        return {name: getattr(s, name) for name, _ in s._fields_}
+
+    def drain(self, timeout: float = -1.0) -> None:
+        _check(LIB.gg_server_drain(self._h, timeout))
+
+    def close(self) -> None:
+        if self._h:
+            LIB.gg_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def kernel_launches() -> int:

@@ -119,6 +119,45 @@ def tile_sort(uv: np.ndarray, img_dim: int, tile: int = 32, gcf_dim: int = 8,
     return np.argsort(key, kind="stable")
 
 
+def track_pool(sides=(256, 512, 1024, 2048), nsets: int = 8,
+               pool_len: int = 1_000_000, seed: int = 0, nant: int = 64):
+    """Per grid side, `nsets` independent track observations (different
+    antenna layouts) of `pool_len` visibilities each: {side: (uv[nsets,
+    pool_len, 2] float64, vals[nsets, pool_len] complex64)}.  Requests of
+    the batched and served workloads are slices of these."""
+    nbl = nant * (nant - 1) // 2
+    ntime = -(-pool_len // nbl)
+    pools = {}
+    for i, N in enumerate(sides):
+        uvs, vs = [], []
+        for s in range(nsets):
+            uv, v = tracks(N, nant=nant, ntime=ntime, npts=pool_len,
+                           seed=seed * 1000 + i * 100 + s)
+            uvs.append(uv)
+            vs.append(v)
+        pools[N] = (np.stack(uvs), np.stack(vs))
+    return pools
+
+
+def request_specs(n: int, seed: int = 0, sides=(256, 512, 1024, 2048),
+                  supports=(8, 16), nvis_min: float = 1e4, nvis_max: float = 1e6,
+                  log10_mean: float = 5.0, log10_sd: float = 0.5,
+                  nsets: int = 8, pool_len: int = 1_000_000):
+    """Job / request shapes of the batched and served workloads: grid side
+    uniform over `sides`, support uniform over `supports`, visibility count
+    lognormal (log10 ~ N(log10_mean, log10_sd)) clipped to [nvis_min,
+    nvis_max], and a random slice of one pool track set."""
+    rng = np.random.default_rng(seed)
+    side = rng.choice(np.asarray(sides), n)
+    S = rng.choice(np.asarray(supports), n)
+    nvis = np.clip(10.0 ** rng.normal(log10_mean, log10_sd, n), nvis_min,
+                   nvis_max).astype(np.int64)
+    tset = rng.integers(0, nsets, n)
+    off = (rng.random(n) * (pool_len - nvis + 1)).astype(np.int64)
+    return {"side": side.astype(np.int64), "S": S.astype(np.int64), "nvis": nvis,
+            "set": tset.astype(np.int64), "offset": off}
+
+
 def gaussian_gcf_1d(gcf_dim: int, oversample: int = 8,
                     sigma: float | None = None) -> np.ndarray:
     """[G][S] factors g(a' - S/2 + 1 - s/G), g(x) = exp(-x^2 / (2 sigma^2))"""

@@ -67,6 +67,47 @@ int main() {
         assert r.returncode == 3 and "gridGPU:" in r.stderr
 
 
+def test_struct_layouts_match_header(tmp_path):
+    """ctypes mirrors of the ABI structs have the C sizes and field offsets."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc")
+    if not cc:
+        pytest.skip("no gcc")
+    structs = {"gg_options": gg.gg_options, "gg_job": gg.gg_job,
+               "gg_request": gg.gg_request, "gg_result": gg.gg_result,
+               "gg_server_config": gg.gg_server_config,
+               "gg_server_stats": gg.gg_server_stats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gg.h"', 'int main(void){']
+    for name, cls in structs.items():
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'printf("{name}.{fname} %zu\\n", offsetof({name}, {fname}));')
+    lines.append("return 0;}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    r = subprocess.run([cc, "-std=c99", str(src), "-I", os.path.join(ROOT, "include"),
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True,
+                                                 text=True).stdout.splitlines())
+    for name, cls in structs.items():
+        assert int(got[name]) == ctypes.sizeof(cls), name
+        for fname, _ in cls._fields_:
+            assert int(got[f"{name}.{fname}"]) == getattr(cls, fname).offset, (name, fname)
+
+
+def test_server_config_defaults():
+    c = gg.gg_server_config()
+    assert gg.LIB.gg_server_default_config(ctypes.byref(c)) == gg.OK
+    assert c.streams == 2 and c.max_batch_jobs == 256 and c.hbm_budget_bytes == 150000000000
+    assert c.options.mode == gg.MODE_WINDOW and c.options.accum == gg.ACC_COMPENSATED
+    c.streams = 0
+    h = ctypes.c_void_p()
+    assert gg.LIB.gg_server_create(ctypes.byref(h), ctypes.byref(c)) == gg.ERR_ARG
+
+
 def test_abi_version_and_defaults():
     assert gg.LIB.gg_abi_version() == 1
     o = gg.gg_options()
