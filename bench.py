@@ -55,9 +55,11 @@ FALLBACK_HBM_GBS = 6800.0
 
 STREAM_DESC = ("grid side uniform in {256,512,1024,2048}; support 8 or 16, "
                "oversample 8; visibility count lognormal (log10 ~ N(5, 0.5)) "
-               "clipped to [1e4, 1e6]; each a slice of one of 8 synthetic "
-               "uv-track observations per grid side (64 antennas in a 2 km "
-               "disk, dec -30 deg, 90% fill); complex64 N(0,1) values; FP64 "
+               "clipped to [1e4, 1e6]; each a contiguous slice (whole baseline "
+               "tracks) of one of 8 synthetic observations per grid side with "
+               "the tracks4096 geometry (64 antennas at random positions in a "
+               "2 km disk, 2016 baselines x 2080 samples over +-4 h, dec -30 "
+               "deg, 90% fill); complex64 N(0,1) values; FP64 "
                "u,v; complex64 grids; FP32 compensated accumulation; "
                "tabulated separable Gaussian GCFs resident on the device")
 
@@ -309,7 +311,7 @@ def run_served(args, rank, world, local_rank, dist):
     zeros = np.zeros(n)
     for _ in range(args.warmup):
         stream(zeros)
-    # timed saturation passes (all arrivals at t=0); L2: the 768 MB of input
+    # timed saturation passes (all arrivals at t=0); L2: the 3.2 GB of input
     # pools exceed it
     if dist:
         dist.barrier()
@@ -463,7 +465,7 @@ def run_served(args, rank, world, local_rank, dist):
                    "visibilities_per_step": total_vis, "requests": n,
                    "server": {"streams": w["streams"], "max_batch_jobs": w["max_batch_jobs"],
                               "hbm_budget_bytes": int(w["budget"]), "method": "window"},
-                   "l2": "inputs (768 MB of track pools) exceed L2",
+                   "l2": "inputs (3.2 GB of track pools) exceed L2",
                    "timing": "server clock from first arrival to last grid ready, "
                              "per pass; device synchronised around the passes",
                    "parallelism": f"replicas x{world}"},

@@ -13,7 +13,9 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -191,6 +193,16 @@ struct Plan {
   std::vector<std::pair<void *, size_t>> zero_ranges;  // outputs to clear
   std::vector<std::pair<float *, int64_t>> finalize;   // (out, floats) comp scatter
   std::vector<std::pair<void *, int64_t>> count_fill;  // (vals, npts) DEBUG1
+  // row-doubled GCF tables read by the moving-window kernel: source (null:
+  // the DEBUG1 count table), workspace offset, support; per job (class
+  // order) the offset of its copy, or SIZE_MAX
+  struct GcfCopy {
+    const void *src;
+    size_t off;
+    int S;
+  };
+  std::vector<GcfCopy> gcf_copies;
+  std::vector<size_t> hgcf_off;
   // workspace carve (offsets into the device workspace)
   size_t o_jobs, o_bin, o_visb, o_tileb, o_class, o_packed, o_key, o_bm,
       o_cursor, o_scan, o_sidx, o_svals, o_order, o_items, o_kept, o_lo,
@@ -347,8 +359,9 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
   pl.mode = mode;
   if (mode == GG_MODE_WINDOW) {
     for (int j = 0; j < njobs; ++j) {
-      const size_t need = window_smem_bytes((int)jobs[j].gcf_dim, opt->accum,
-                                            vt == GG_C128, pl.T, pl.group_warps);
+      const size_t need = window_smem_bytes((int)jobs[j].gcf_dim, opt->accum, vt == GG_C128,
+                                            pl.T, pl.group_warps,
+                                            opt->gcf_kind == GG_GCF_GAUSSIAN);
       if (need > 227 * 1024)
         return fail(GG_ERR_ARG,
                     "tile %d with support %lld needs %zu bytes of shared memory "
@@ -401,6 +414,22 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
       if (jobs[j].out_type == GG_C64)
         lo_total += align256(8 * (size_t)pl.P * jobs[j].img_dim * jobs[j].img_dim);
   pl.o_lo = pl.comp_lo ? take(lo_total) : 0;
+  pl.gcf_copies.clear();
+  pl.hgcf_off.assign(njobs, SIZE_MAX);
+  if (mode == GG_MODE_WINDOW && !pl.gauss) {
+    std::map<std::pair<const void *, int>, size_t> seen;
+    for (int k = 0; k < njobs; ++k) {
+      const gg_job &J = jobs[order[k]];
+      const std::pair<const void *, int> key(count ? nullptr : J.gcf, (int)J.gcf_dim);
+      auto it = seen.find(key);
+      if (it == seen.end()) {
+        const size_t o = take(gcf_double_rows_bytes(key.second, pl.G, (int)vbytes));
+        it = seen.emplace(key, o).first;
+        pl.gcf_copies.push_back({key.first, o, key.second});
+      }
+      pl.hgcf_off[k] = it->second;
+    }
+  }
   pl.ws_bytes = off;
 
   // host tables in class order
@@ -506,6 +535,7 @@ static void plan_bind(const gg_options *opt, Plan &pl, char *ws, char *host) {
       pl.hbin[k].vals = cv;
       D.gcf = ws + pl.o_count_gcf;
     }
+    if (pl.hgcf_off[k] != SIZE_MAX) D.gcf = ws + pl.hgcf_off[k];
     if (binned) {
       D.idx = (const int2 *)(ws + pl.o_sidx);
       D.vals = ws + pl.o_svals;
@@ -565,6 +595,9 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
                                   k == 0 ? (int64_t)pl.G * pl.G * maxS * maxS : 0, s));
     }
   }
+  for (const auto &c : pl.gcf_copies)
+    GG_CUDA(launch_gcf_double_rows(c.src ? c.src : ws + pl.o_count_gcf, ws + c.off, c.S, pl.G,
+                                   (int)vbytes, s));
 
   GridLaunch g{};
   g.accum = pl.accum;

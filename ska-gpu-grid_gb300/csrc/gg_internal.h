@@ -98,6 +98,13 @@ struct GridLaunch {
 
 cudaError_t launch_scatter(const GridLaunch &g, cudaStream_t s);
 cudaError_t launch_window(const GridLaunch &g, cudaStream_t s);
+// Row-doubled copy of a [G*G][S][S] GCF table for the moving-window kernel:
+// dst[s][b][a] = src[s][b mod S][a] for b < 2S (elem_bytes 8 or 16)
+cudaError_t launch_gcf_double_rows(const void *src, void *dst, int S, int G,
+                                   int elem_bytes, cudaStream_t s);
+inline size_t gcf_double_rows_bytes(int S, int G, int elem_bytes) {
+  return (size_t)elem_bytes * G * G * 2 * S * S;
+}
 cudaError_t launch_gather(const GridLaunch &g, cudaStream_t s);
 // compensated scatter with complex64 output: out = fl(hi + lo)
 cudaError_t launch_comp_finalize(float *out, const float *lo, int64_t n,
@@ -107,6 +114,6 @@ cudaError_t launch_comp_finalize(float *out, const float *lo, int64_t n,
 cudaError_t launch_count_inputs(void *vals, int vals_f64, int64_t npts, int P,
                                 void *gcf, int64_t gcf_elems, cudaStream_t s);
 // smem bytes the window kernel needs (for occupancy sizing)
-size_t window_smem_bytes(int S, int accum, int vals_f64, int T, int group_warps);
+size_t window_smem_bytes(int S, int accum, int vals_f64, int T, int group_warps, int gauss);
 
 }  // namespace gg

@@ -53,12 +53,14 @@ struct GcfSrc<S, true, VT> {
   }
 };
 
-// g1[s][a'] = exp(-(a' - S/2 + 1 - s/G)^2 / (2 sigma^2)) in FP32
+// g1[s][a'] = exp(-(a' - S/2 + 1 - s/G)^2 / (2 sigma^2)) in FP32, rows of
+// `row` entries (row = 2S repeats each row once: g1[s][a' + S] = g1[s][a'])
 __device__ __forceinline__ void gauss_fill(float *g1, int S, int G, float sigma,
-                                           int tid, int nt) {
+                                           int tid, int nt, int row = 0) {
+  if (row == 0) row = S;
   const float inv = 1.0f / (2.0f * sigma * sigma);
-  for (int i = tid; i < G * S; i += nt) {
-    int s = i / S, ap = i % S;
+  for (int i = tid; i < G * row; i += nt) {
+    int s = i / row, ap = (i % row) % S;
     float x = (float)(ap - S / 2 + 1) - (float)s / (float)G;
     g1[i] = expf(-(x * x) * inv);
   }

@@ -12,8 +12,9 @@
 //
 // Limits: at most kNoAllocMaxVis visibilities, img_dim up to 4096 with the
 // default 32-cell tile (kNoAllocMaxTiles uv tiles), one polarisation,
-// complex64 values.  The array (about 9 MiB) is held by every GPU that loads
-// this library until the process exits.
+// complex64 values, a GCF table of at most 65536 taps (G*G*S*S).  The array
+// (about 10 MiB) is held by every GPU that loads this library until the
+// process exits.
 //
 // Set-up: the first call on a device looks up the device address of the
 // array with cudaGetSymbolAddress while that device is current, and caches
@@ -56,7 +57,11 @@ constexpr size_t kOffKept = kOffScan + al(sizeof(int) * kScanInts);
 constexpr size_t kOffSidx = kOffKept + al(sizeof(int) * (kNoAllocMaxVis + 8));
 constexpr size_t kOffSvals = kOffSidx + al(sizeof(int2) * (kNoAllocMaxVis + 8));
 constexpr size_t kOffItems = kOffSvals + al(sizeof(float2) * (kNoAllocMaxVis + 8) + 64);
-constexpr size_t kScratchBytes = kOffItems + al(sizeof(WorkItem) * 4 * kClassCap);
+// row-doubled copy of the GCF table read by the window kernel: up to
+// kNoAllocMaxGcf sub-kernel taps (G*G*S*S), complex64
+constexpr int64_t kNoAllocMaxGcf = 1 << 16;
+constexpr size_t kOffGcf = kOffItems + al(sizeof(WorkItem) * 4 * kClassCap);
+constexpr size_t kScratchBytes = kOffGcf + al(sizeof(float2) * 2 * kNoAllocMaxGcf);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -121,6 +126,10 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
     return noalloc_fail(GG_ERR_ARG,
                         "noalloc: img_dim exceeds the fixed scratch (max 16384 uv tiles, "
                         "i.e. 4096 at tile 32)");
+  if (opt->gcf_kind == GG_GCF_TABLE && (int64_t)G * G * S * S > kNoAllocMaxGcf)
+    return noalloc_fail(GG_ERR_ARG,
+                        "noalloc: GCF table exceeds the fixed scratch (G*G*S*S at most 65536, "
+                        "e.g. oversample 8 with support 32)");
   if (!job->out || (n > 0 && (!job->uv || !job->vals)) ||
       (opt->gcf_kind == GG_GCF_TABLE && !job->gcf))
     return noalloc_fail(GG_ERR_ARG, "noalloc: null buffer");
@@ -140,7 +149,7 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   std::memset(&D, 0, sizeof D);
   D.out = job->out;
   D.uv = job->uv;
-  D.gcf = job->gcf;
+  D.gcf = opt->gcf_kind == GG_GCF_TABLE ? (const void *)(ws + kOffGcf) : nullptr;
   D.idx = (const int2 *)(ws + kOffSidx);
   D.vals = ws + kOffSvals;
   D.bookmarks = (const int *)(ws + kOffBm);
@@ -195,6 +204,9 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   GG_NA(cudaMemsetAsync(flags, 0, 16 * sizeof(int), s));
   const size_t out_bytes = (size_t)(D.out_f64 ? 16 : 8) * N * N;
   GG_NA(cudaMemsetAsync(job->out, 0, out_bytes, s));
+
+  if (opt->gcf_kind == GG_GCF_TABLE)
+    GG_NA(launch_gcf_double_rows(job->gcf, ws + kOffGcf, (int)S, G, 8, s));
 
   BinBuffers b{};
   b.jobs = (const BinJob *)(ws + kOffBin);

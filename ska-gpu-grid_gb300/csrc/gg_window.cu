@@ -18,9 +18,10 @@
 //    same and, when it changes, adds the sum into the sub-grid.  Ownership
 //    makes that read-modify-write exclusive: no atomics, and no
 //    synchronisation between visibilities.
-//  * FP32 sums are compensated: a (hi, lo) pair per component updated with
-//    Knuth's TwoSum on the packed (re, im) pair (f32x2 instructions), in
-//    registers and again when a register sum is added into the sub-grid.
+//  * FP32 sums are compensated: sub-grid cells hold a (hi, lo) pair per
+//    component, updated with Knuth's TwoSum on the packed (re, im) pair
+//    (f32x2 instructions) whenever a register run is added in; register runs
+//    are cut after kRunMax records, which bounds their plain-FP32 error.
 //  * Visibility records (packed indices + values) stream through shared
 //    memory by 1-D TMA bulk copies, double-buffered, as one continuous stream
 //    across work items (the next item is claimed early and its first chunk
@@ -28,6 +29,10 @@
 //  * Once per item the sub-grid is flushed to HBM with native vector
 //    reductions (touched cells only) and zeroed as it is read.  Items too
 //    sparse to pay for that flush send each register sum straight to HBM.
+#include <algorithm>
+#include <climits>
+#include <type_traits>
+
 #include "gg_kernels.cuh"
 
 namespace gg {
@@ -92,29 +97,25 @@ template <> struct WinAcc<0> {
     out_red(J, cell, p, P, (double)v.x, (double)v.y);
   }
 };
+// Compensated: a register run of at most kRunMax records is summed plainly in
+// FP32 and every run is added into a two-sum (hi, lo) cell, so the rounding
+// error is that of one short run per cell plus O(u^2) terms, not O(n u).
 template <> struct WinAcc<1> {
   using VT = float;
   using CellT = float4;
-  u64 hi, lo;
-  __device__ __forceinline__ void zero() { hi = lo = 0ull; }
-  __device__ __forceinline__ void add(u64 t) {
-    u64 e;
-    hi = two_sum2(hi, t, e);
-    lo = add2(lo, e);
-  }
+  u64 s;
+  __device__ __forceinline__ void zero() { s = 0ull; }
+  __device__ __forceinline__ void add(u64 t) { s = add2(s, t); }
   __device__ __forceinline__ void into(CellT *c) const {
     const float4 o = *c;
     u64 e;
-    const u64 h = two_sum2(pk2(o.x, o.y), hi, e);
-    const float2 hf = upk2(h), lf = upk2(add2(pk2(o.z, o.w), add2(e, lo)));
+    const u64 h = two_sum2(pk2(o.x, o.y), s, e);
+    const float2 hf = upk2(h), lf = upk2(add2(pk2(o.z, o.w), e));
     *c = make_float4(hf.x, hf.y, lf.x, lf.y);
   }
   __device__ __forceinline__ void out(const JobDesc &J, size_t cell, int p, int P) const {
-    const float2 h = upk2(hi), l = upk2(lo);
-    if (J.out_f64)
-      out_red(J, cell, p, P, (double)h.x + (double)l.x, (double)h.y + (double)l.y);
-    else
-      out_red(J, cell, p, P, (double)__fadd_rn(h.x, l.x), (double)__fadd_rn(h.y, l.y));
+    const float2 v = upk2(s);
+    out_red(J, cell, p, P, (double)v.x, (double)v.y);
   }
 };
 template <> struct WinAcc<2> {
@@ -161,6 +162,9 @@ __device__ __forceinline__ void out_cell(const JobDesc &J, size_t cell, int p,
 
 // ---- configuration ----------------------------------------------------------------
 constexpr int kWinThreads = 256;
+// longest register run (records) of the compensated mode: a run of L terms
+// carries at most about L/2 units in the last place of relative error
+constexpr int kRunMax = 32;
 
 // warps per sub-grid group chosen when the caller leaves it open
 // (measured on the 4096^2 track workload: S=8 with 2 warps per group beats 1)
@@ -173,16 +177,20 @@ template <int S, int W> struct WinCfg {
   static constexpr int Q = (S * S + NGT - 1) / NGT;          // residues per thread
   static constexpr int K = S >= 32 ? 512 : (S >= 16 ? 256 : 128);  // records per chunk
   static constexpr int GROUPS = kWinThreads / NGT;
+  // resident CTAs per SM the register allocation is held to (shared memory
+  // allows as many at the default tile sizes)
+  static constexpr int MIN_CTAS = S <= 8 ? 3 : (S <= 16 ? 2 : 1);
 };
 
-template <int S, int W, int MODE>
+template <int S, int W, int MODE, bool GAUSS>
 struct WinLayout {
   using Cfg = WinCfg<S, W>;
   using VT2 = typename vec2_of<typename WinAcc<MODE>::VT>::type;
   using CellT = typename WinAcc<MODE>::CellT;
   static constexpr int IDX_BUF = Cfg::K * 8 + 16;
   static constexpr int VAL_BUF = Cfg::K * (int)sizeof(VT2) + 16;
-  static constexpr int G1_BYTES = 64 * S * 4;
+  // 1-D Gaussian factors (computed GCF only): doubled rows, G <= 64
+  static constexpr int G1_BYTES = GAUSS ? 64 * 2 * S * 4 : 0;
   // per group: 2 mbarriers (16 B), 2 index buffers, 2 value buffers, sub-grid
   __host__ __device__ static size_t group_bytes(int T) {
     const size_t R = (size_t)T + S - 1;
@@ -202,10 +210,10 @@ __device__ __forceinline__ void group_sync(int gid, int nthreads) {
 }
 
 template <int S, int W, int MODE, bool GAUSS>
-__global__ void __launch_bounds__(kWinThreads)
+__global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
     window_kernel(KParams kp) {
   using Cfg = WinCfg<S, W>;
-  using L = WinLayout<S, W, MODE>;
+  using L = WinLayout<S, W, MODE, GAUSS>;
   using ACC = WinAcc<MODE>;
   using VT2 = typename L::VT2;
   using CellT = typename L::CellT;
@@ -248,7 +256,7 @@ __global__ void __launch_bounds__(kWinThreads)
     s_item[gid] = a;
     s_next[gid] = a < nitems ? atomicAdd(kp.item_next, 1) : nitems;
   }
-  if constexpr (GAUSS) gauss_fill(g1, S, kp.G, kp.sigma, tid, kWinThreads);
+  if constexpr (GAUSS) gauss_fill(g1, S, kp.G, kp.sigma, tid, kWinThreads, 2 * S);
   for (int i = gt; i < R * R; i += NGT) region[i] = CellT{};
   __syncthreads();
 
@@ -286,7 +294,6 @@ __global__ void __launch_bounds__(kWinThreads)
     const int n = w.end - w.start;
     const int nch = (n + K - 1) / K;
     const bool direct = (long long)n * S * S < (long long)R * R;
-    const int lim = direct ? N : R;
     // what follows in the stream: the next plane of this item, or the next item
     const int nxt_item = p + 1 < P ? item : next;
     const int nxt_p = p + 1 < P ? p + 1 : 0;
@@ -307,13 +314,30 @@ __global__ void __launch_bounds__(kWinThreads)
 
     const VT2 *gtab = reinterpret_cast<const VT2 *>(J.gcf);
     const int G = J.G;
+    // tiles on the border of the grid hold the clamped mains, whose
+    // footprints may leave the sub-grid
+    const bool edge = tx == 0 || ty == 0 || tx == J.ntx - 1 || ty == J.ntx - 1;
     ACC acc[Q];
     int cur[Q];
+    // footprint origin of the last record, this thread's column in it and
+    // the offset of its first tap in a sub-kernel of the row-doubled table
+    int pfx = INT_MIN, pfy = INT_MIN, pax = 0, pofs = 0, pkx = 0, pky = 0;
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
       acc[k].zero();
       cur[k] = -1;
     }
+    int run = 0;  // records in the current register runs (compensated mode)
+    auto flush_runs = [&]() {
+      run = 0;
+#pragma unroll
+      for (int k = 0; k < Q; ++k)
+        if (cur[k] >= 0) {
+          if (direct) acc[k].out(J, (size_t)cur[k], p, P);
+          else acc[k].into(region + cur[k]);
+          acc[k].zero();
+        }
+    };
 
     for (int c = 0; c < nch; ++c) {
       const int g = gfirst + c, b = g & 1;
@@ -326,89 +350,173 @@ __global__ void __launch_bounds__(kWinThreads)
       const int2 *ib = reinterpret_cast<const int2 *>(idx0 + b * L::IDX_BUF + (((size_t)s0 * 8) & 15));
       const VT2 *vb = reinterpret_cast<const VT2 *>(val0 + b * L::VAL_BUF +
                                                     (((size_t)s0 * sizeof(VT2)) & 15));
-      // Two-stage pipeline over the chunk's records: stage A decodes record
-      // r+1 (target cells, value) and issues its GCF loads; stage B adds
-      // record r into the register sums.  The GCF load latency of one record
-      // is hidden behind the accumulation of the previous one.
+      // Interior tiles.  Records come in runs whose footprint origin does
+      // not move (the same target cell for every residue); the slow step
+      // handles the first record of a run (target cells, flushes of the
+      // register sums whose cell changed), the fast loop only adds records
+      // while the origin stays put.  Both decisions are uniform over the
+      // group.  The fast loop is unrolled by two with two register stages:
+      // it decodes record r+1 and issues its GCF loads before adding record
+      // r, so that a record's load latency is hidden behind the previous one.
       using GT = typename vec2_of<typename ACC::VT>::type;
-      auto run_chunk = [&](auto dir_tag) {
-        constexpr bool D = decltype(dir_tag)::value;  // direct (sparse) item
-        int lcA[Q];
-        GT gA[Q];
-        VT2 vA;
-        auto stageA = [&](int r) {
+      // The GCF table seen here repeats every sub-kernel's rows once
+      // ([G*G][2S][S]): this thread's Q taps of a record, rows b0 + k*D mod S,
+      // then sit at fixed strides k*D*S from its first tap.
+      constexpr int D = NGT / S;
+      auto load_g = [&](GT (&g)[Q], int sx, int sy) {
+        if constexpr (GAUSS) {
+          const float gxf = g1[sx * 2 * S + pax];
+          const float *gy = g1 + sy * 2 * S + pofs;
+#pragma unroll
+          for (int k = 0; k < Q; ++k) {
+            g[k].x = (typename ACC::VT)(gxf * gy[k * D]);
+            g[k].y = 0;
+          }
+        } else {
+          const GT *gp = reinterpret_cast<const GT *>(gtab) + (sy * G + sx) * (2 * S * S) + pofs;
+#pragma unroll
+          for (int k = 0; k < Q; ++k) g[k] = __ldg(gp + k * D * S);
+        }
+      };
+      auto accum = [&](const GT (&g)[Q], const VT2 v) {
+        u64 vrr = 0, vsn = 0, vv = 0;
+        if constexpr (MODE != 2) {
+          vv = pk2((float)v.x, (float)v.y);
+          vrr = pk2((float)v.x, (float)v.x);
+          vsn = pk2(-(float)v.y, (float)v.y);
+        }
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+          if (S * S % NGT != 0 && !rv[k]) continue;
+          if constexpr (MODE == 2) {
+            acc[k].add(v.x * g[k].x - v.y * g[k].y, v.x * g[k].y + g[k].x * v.y);
+          } else if constexpr (GAUSS) {
+            acc[k].add(mul2(vv, pk2((float)g[k].x, (float)g[k].x)));
+          } else {
+            acc[k].add(fma2(vrr, pk2((float)g[k].x, (float)g[k].y),
+                            mul2(vsn, pk2((float)g[k].y, (float)g[k].x))));
+          }
+        }
+      };
+      // One step of the fast loop: add record r (stage a).  Record r+1 is in
+      // stage b and continues the run when `nb`.  Record r+2 is decoded and
+      // loaded into stage c whether or not it continues the run (index
+      // clamped to the chunk; a wasted load at a run's end costs less than
+      // a branch around it), and `nc` says whether it does: same footprint
+      // origin and inside `mr`, the chunk end or the run-length limit.
+      // Loads run two records ahead of their use.
+      auto step = [&](int r, int mr, const GT (&ga)[Q], const VT2 va, GT (&gc)[Q], VT2 &vc,
+                      bool &nc) {
+        const int r2 = min(r + 2, m - 1);
+        const int2 q = ib[r2];
+        vc = vb[r2];
+        nc = (((q.x ^ pkx) | (q.y ^ pky)) & ~(G - 1)) == 0 && r + 2 < mr;
+        load_g(gc, unpack_sub(q.x, log2G), unpack_sub(q.y, log2G));
+        accum(ga, va);
+      };
+      auto run_interior = [&]() {
+        int r = 0;
+        while (r < m) {
+          // slow step: record r opens a run
           const int2 pk = ib[r];
-          vA = vb[r];
+          VT2 va = vb[r], vb1, vc1;
+          const int fx0 = unpack_main(pk.x, log2G) - H + 1;
+          const int fy0 = unpack_main(pk.y, log2G) - H + 1;
+          if (MODE == 1 && run >= kRunMax) flush_runs();
+          if (fx0 != pfx || fy0 != pfy) {
+            pfx = fx0;
+            pfy = fy0;
+            pax = (rx - fx0) & (S - 1);
+            const int b0 = (ry[0] - fy0) & (S - 1);
+            pofs = GAUSS ? b0 : b0 * S + pax;
+            const int lx = fx0 + pax - ox;
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+              const int bp = (b0 + k * D) & (S - 1);
+              const int lc = (S * S % NGT == 0 || rv[k]) ? (fy0 + bp - oy) * R + lx : -1;
+              if (lc != cur[k]) {
+                if (cur[k] >= 0) acc[k].into(region + cur[k]);
+                cur[k] = lc;
+                acc[k].zero();
+              }
+            }
+          }
+          // the packed main cells of this run (the oversample bits masked
+          // out when comparing) and the last record the run may reach
+          pkx = pk.x;
+          pky = pk.y;
+          const int r0 = r;
+          const int mr = MODE == 1 ? min(m, r0 + (kRunMax - run)) : m;
+          GT ga[Q], gb[Q], gc[Q];
+          load_g(ga, unpack_sub(pk.x, log2G), unpack_sub(pk.y, log2G));
+          const int r1 = min(r + 1, m - 1);
+          const int2 q = ib[r1];
+          vb1 = vb[r1];
+          bool nb = (((q.x ^ pkx) | (q.y ^ pky)) & ~(G - 1)) == 0 && r + 1 < mr, nc, na;
+          load_g(gb, unpack_sub(q.x, log2G), unpack_sub(q.y, log2G));
+          // fast loop over the rest of the run, three rotating stages
+          for (;;) {
+            step(r++, mr, ga, va, gc, vc1, nc);
+            if (!nb) break;
+            step(r++, mr, gb, vb1, ga, va, na);
+            if (!nc) break;
+            step(r++, mr, gc, vc1, gb, vb1, nb);
+            if (!na) break;
+          }
+          run += r - r0;
+        }
+      };
+      // Edge tiles and sparse items (a small share of the taps) take a plain
+      // one-stage loop with bounds tests: it keeps the register footprint of
+      // the kernel at that of the interior path.
+      auto run_checked = [&]() {
+        const int LIM = direct ? N : R;
+        const int bx = direct ? 0 : ox, by = direct ? 0 : oy;
+        for (int r = 0; r < m; ++r) {
+          if (MODE == 1 && ++run >= kRunMax) flush_runs();
+          const int2 pk = ib[r];
+          const VT2 v = vb[r];
           const int mx = unpack_main(pk.x, log2G), sx = unpack_sub(pk.x, log2G);
           const int my = unpack_main(pk.y, log2G), sy = unpack_sub(pk.y, log2G);
           const int fx0 = mx - H + 1, fy0 = my - H + 1;
           const int ap = (rx - fx0) & (S - 1);
-          const int lx = fx0 + ap - (D ? 0 : ox);
-          const bool xin = (unsigned)lx < (unsigned)(D ? N : R);
-          const VT2 *gk = GAUSS ? nullptr : gtab + ((sy * G + sx) * S * S + ap);
-          const float gxf = GAUSS ? g1[sx * S + ap] : 0.f;
+          const int lx = fx0 + ap - bx;
+          const bool xin = (unsigned)lx < (unsigned)LIM;
 #pragma unroll
           for (int k = 0; k < Q; ++k) {
-            if (S * S % NGT != 0 && !rv[k]) {
-              lcA[k] = -1;
-              continue;
-            }
             const int bp = (ry[k] - fy0) & (S - 1);
-            const int ly = fy0 + bp - (D ? 0 : oy);
-            lcA[k] = (xin && (unsigned)ly < (unsigned)(D ? N : R)) ? ly * (D ? N : R) + lx : -1;
-            if constexpr (GAUSS) {
-              gA[k].x = (typename ACC::VT)(gxf * g1[sy * S + bp]);
-              gA[k].y = 0;
-            } else {
-              gA[k] = __ldg(reinterpret_cast<const GT *>(gk) + bp * S);
-            }
-          }
-        };
-        if (m > 0) stageA(0);
-#pragma unroll 2
-        for (int r = 0; r < m; ++r) {
-          int lcB[Q];
-          GT gB[Q];
-#pragma unroll
-          for (int k = 0; k < Q; ++k) {
-            lcB[k] = lcA[k];
-            gB[k] = gA[k];
-          }
-          const VT2 v = vA;
-          if (r + 1 < m) stageA(r + 1);
-          u64 vv = 0, vrr = 0, vsn = 0;
-          if constexpr (MODE != 2) {
-            vv = pk2((float)v.x, (float)v.y);
-            vrr = pk2((float)v.x, (float)v.x);
-            vsn = pk2(-(float)v.y, (float)v.y);
-          }
-#pragma unroll
-          for (int k = 0; k < Q; ++k) {
-            const int lc = lcB[k];
+            const int ly = fy0 + bp - by;
+            const bool in = (S * S % NGT == 0 || rv[k]) && xin && (unsigned)ly < (unsigned)LIM;
+            const int lc = in ? ly * LIM + lx : -1;
             if (lc != cur[k]) {
-              // register sum -> sub-grid (exclusive) or straight to HBM
               if (cur[k] >= 0) {
-                if (D) acc[k].out(J, (size_t)cur[k], p, P);
+                if (direct) acc[k].out(J, (size_t)cur[k], p, P);
                 else acc[k].into(region + cur[k]);
               }
               cur[k] = lc;
               acc[k].zero();
             }
             if (lc < 0) continue;
-            if constexpr (MODE == 2) {
-              const double gr = gB[k].x, gi = gB[k].y;
-              acc[k].add(v.x * gr - v.y * gi, v.x * gi + gr * v.y);
-            } else if constexpr (GAUSS) {
-              acc[k].add(mul2(vv, pk2((float)gB[k].x, (float)gB[k].x)));
+            GT g;
+            if constexpr (GAUSS) {
+              g.x = (typename ACC::VT)(g1[sx * 2 * S + ap] * g1[sy * 2 * S + bp]);
+              g.y = 0;
             } else {
-              acc[k].add(fma2(vrr, pk2((float)gB[k].x, (float)gB[k].y),
-                              mul2(vsn, pk2((float)gB[k].y, (float)gB[k].x))));
+              g = __ldg(reinterpret_cast<const GT *>(gtab) + (sy * G + sx) * (2 * S * S) +
+                        bp * S + ap);
+            }
+            if constexpr (MODE == 2) {
+              acc[k].add(v.x * g.x - v.y * g.y, v.x * g.y + g.x * v.y);
+            } else {
+              const u64 vrr = pk2((float)v.x, (float)v.x), vsn = pk2(-(float)v.y, (float)v.y);
+              acc[k].add(fma2(vrr, pk2((float)g.x, (float)g.y),
+                              mul2(vsn, pk2((float)g.y, (float)g.x))));
             }
           }
         }
       };
-      if (direct) run_chunk(std::true_type{});
-      else run_chunk(std::false_type{});
+      if (direct || edge) run_checked();
+      else run_interior();
       group_sync(gid, NGT);  // buffer b consumed by the whole group
       if (leader) issue_next(g + 3);
     }
@@ -454,7 +562,7 @@ __global__ void __launch_bounds__(kWinThreads)
 
 template <int S, int W, int MODE, bool GAUSS>
 static cudaError_t win_launch(const KParams &kp, int sm_count, cudaStream_t s) {
-  using L = WinLayout<S, W, MODE>;
+  using L = WinLayout<S, W, MODE, GAUSS>;
   const size_t smem = L::cta_bytes(kp.T);
   auto kern = window_kernel<S, W, MODE, GAUSS>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -494,13 +602,18 @@ static int win_warps(int S, int requested) {
   return w;
 }
 
-size_t window_smem_bytes(int S, int accum, int vals_f64, int T, int group_warps) {
+size_t window_smem_bytes(int S, int accum, int vals_f64, int T, int group_warps, int gauss) {
   const int mode = vals_f64 ? 2 : (accum == GG_ACC_COMPENSATED ? 1 : 0);
   const int w = win_warps(S, group_warps);
+#define GG_WSG(SV, WV, MV)                                                 \
+  return gauss ? WinLayout<SV, WV, MV, true>::cta_bytes(T)                 \
+               : WinLayout<SV, WV, MV, false>::cta_bytes(T)
 #define GG_WS(SV, WV)                                                      \
-  return mode == 2 ? WinLayout<SV, WV, 2>::cta_bytes(T)                    \
-                   : (mode == 1 ? WinLayout<SV, WV, 1>::cta_bytes(T)       \
-                                : WinLayout<SV, WV, 0>::cta_bytes(T))
+  do {                                                                     \
+    if (mode == 2) GG_WSG(SV, WV, 2);                                      \
+    if (mode == 1) GG_WSG(SV, WV, 1);                                      \
+    GG_WSG(SV, WV, 0);                                                     \
+  } while (0)
   switch (S) {
     case 4: GG_WS(4, 1);
     case 8:
@@ -515,7 +628,33 @@ size_t window_smem_bytes(int S, int accum, int vals_f64, int T, int group_warps)
       GG_WS(32, 4);
   }
 #undef GG_WS
+#undef GG_WSG
   return 0;
+}
+
+__global__ void __launch_bounds__(256)
+    gcf_double_rows_kernel(const unsigned char *src, unsigned char *dst, int S, int GG,
+                           int elem_bytes) {
+  const int64_t per = 2ll * S * S, n = (int64_t)GG * per;
+  for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) {
+    const int64_t sk = i / per;
+    const int rem = (int)(i % per), b = rem / S, a = rem % S;
+    const int64_t j = (sk * S + (b % S)) * S + a;
+    if (elem_bytes == 16)
+      reinterpret_cast<double2 *>(dst)[i] = reinterpret_cast<const double2 *>(src)[j];
+    else
+      reinterpret_cast<float2 *>(dst)[i] = reinterpret_cast<const float2 *>(src)[j];
+  }
+}
+
+cudaError_t launch_gcf_double_rows(const void *src, void *dst, int S, int G, int elem_bytes,
+                                   cudaStream_t s) {
+  const int64_t n = 2ll * G * G * S * S;
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 1184);
+  gcf_double_rows_kernel<<<blocks, 256, 0, s>>>((const unsigned char *)src, (unsigned char *)dst,
+                                                 S, G * G, elem_bytes);
+  count_launch();
+  return cudaGetLastError();
 }
 
 cudaError_t launch_window(const GridLaunch &g, cudaStream_t s) {

@@ -119,19 +119,20 @@ def tile_sort(uv: np.ndarray, img_dim: int, tile: int = 32, gcf_dim: int = 8,
     return np.argsort(key, kind="stable")
 
 
-def track_pool(sides=(256, 512, 1024, 2048), nsets: int = 8,
-               pool_len: int = 1_000_000, seed: int = 0, nant: int = 64):
-    """Per grid side, `nsets` independent track observations (different
-    antenna layouts) of `pool_len` visibilities each: {side: (uv[nsets,
-    pool_len, 2] float64, vals[nsets, pool_len] complex64)}.  Requests of
-    the batched and served workloads are slices of these."""
-    nbl = nant * (nant - 1) // 2
-    ntime = -(-pool_len // nbl)
+def track_pool(sides=(256, 512, 1024, 2048), nsets: int = 8, seed: int = 0,
+               nant: int = 64, ntime: int = 2080):
+    """Per grid side, `nsets` independent observations with the track
+    geometry of the 4096^2 workload (nant antennas at random positions in a
+    2 km disk, all baselines, ntime hour-angle samples over +-4 h at dec -30
+    deg, 90% fill), each a different antenna layout: {side: (uv[nsets, nbl *
+    ntime, 2] float64, vals[nsets, nbl * ntime] complex64)}, baseline-major.
+    Jobs of the batched and served workloads are contiguous slices of these
+    (whole baseline tracks at the full time sampling)."""
     pools = {}
     for i, N in enumerate(sides):
         uvs, vs = [], []
         for s in range(nsets):
-            uv, v = tracks(N, nant=nant, ntime=ntime, npts=pool_len,
+            uv, v = tracks(N, nant=nant, ntime=ntime, npts=None,
                            seed=seed * 1000 + i * 100 + s)
             uvs.append(uv)
             vs.append(v)
@@ -142,7 +143,7 @@ def track_pool(sides=(256, 512, 1024, 2048), nsets: int = 8,
 def request_specs(n: int, seed: int = 0, sides=(256, 512, 1024, 2048),
                   supports=(8, 16), nvis_min: float = 1e4, nvis_max: float = 1e6,
                   log10_mean: float = 5.0, log10_sd: float = 0.5,
-                  nsets: int = 8, pool_len: int = 1_000_000):
+                  nsets: int = 8, pool_len: int = 2016 * 2080):
     """Job / request shapes of the batched and served workloads: grid side
     uniform over `sides`, support uniform over `supports`, visibility count
     lognormal (log10 ~ N(log10_mean, log10_sd)) clipped to [nvis_min,
