@@ -183,12 +183,50 @@ def traffic_from_profile(tag):
     return None
 
 
-def roofline(kernel, alg_bytes, kern_ms, tag):
+_RED = {}
+
+
+def red_peaks(dev):
+    """FP32 global-reduction rates of this GPU (libgg_probe.so), once per run:
+    red.global.add.v2.f32 / .f32 per second over an L2-resident array (32 MB),
+    an HBM-sized one (2 GB) and 1024 contended cells."""
+    if _RED:
+        return _RED
+    try:
+        lib = ctypes.CDLL(os.path.join(ROOT, "ska-gpu-grid_gb300", "libgg_probe.so"))
+        lib.gg_probe_red_rate.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_int,
+                                          ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        for name, cells, v2, pat in (("v2_coalesced_l2", 1 << 22, 1, 0),
+                                     ("v2_scattered_l2", 1 << 22, 1, 1),
+                                     ("v2_scattered_hbm", 1 << 28, 1, 1),
+                                     ("v2_contended_1024", 1 << 10, 1, 1),
+                                     ("f32_scattered_l2", 1 << 22, 0, 1)):
+            r = ctypes.c_double()
+            if lib.gg_probe_red_rate(dev, cells, v2, pat, ctypes.byref(r)) == 0:
+                _RED[name] = round(r.value / 1e9, 2)
+    except OSError:
+        pass
+    return _RED
+
+
+def roofline(kernel, alg_bytes, kern_ms, tag, taps=None, dev=0):
     hbm, kind = peaks()
     achieved = alg_bytes / (kern_ms / 1e3) / 1e9
-    return {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": hbm,
-            "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_kind": f"{kind} (copy)",
-            "traffic": traffic_from_profile(tag), "algorithmic_bytes_per_launch": int(alg_bytes)}
+    out = {"bound": "hbm", "kernel": kernel, "achieved": round(achieved, 1), "peak": hbm,
+           "unit": "GB/s", "frac": round(achieved / hbm, 4), "peak_kind": f"{kind} (copy)",
+           "traffic": traffic_from_profile(tag), "algorithmic_bytes_per_launch": int(alg_bytes)}
+    red = red_peaks(dev)
+    if taps and red.get("v2_scattered_l2"):
+        rate = taps / (kern_ms / 1e3) / 1e9
+        out["atomic"] = {
+            "tap_updates_per_s_G": round(rate, 1),
+            "red_v2_peak_G_per_s": red["v2_scattered_l2"],
+            "frac": round(rate / red["v2_scattered_l2"], 3),
+            "note": "grid-tap updates per second of the kernel vs the measured L2 rate of "
+                    "scattered red.global.add.v2.f32, which bounds a scatter gridder "
+                    "(one reduction per tap)",
+            "measured_red_rates_G_per_s": red}
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -405,7 +443,8 @@ def run_served(args, rank, world, local_rank, dist):
     _, kern_ms, _ = ctx.profile_last()
     nv = sum(j.npts for j in jobs)
     alg = nv * 16 + sum(2 * 8 * j.img_dim * j.img_dim for j in jobs)
-    roof = roofline("window_kernel", alg, kern_ms, "window_batch256")
+    taps = sum(j.npts * j.gcf_dim * j.gcf_dim for j in jobs)
+    roof = roofline("window_kernel", alg, kern_ms, "window_batch256", taps, local_rank)
 
     # e2e: inputs from pinned host memory through the server, grids read back
     e2e = None
@@ -580,7 +619,8 @@ def run_batch(args, rank, world, local_rank, dist):
     ctx.grid_batch(opts, jobs)
     _, kern_ms, _ = ctx.profile_last()
     alg = total_vis * 16 + sum(2 * 8 * j.img_dim * j.img_dim for j in jobs)
-    roof = roofline("window_kernel", alg, kern_ms, "window_batch256")
+    taps = sum(j.npts * j.gcf_dim * j.gcf_dim for j in jobs)
+    roof = roofline("window_kernel", alg, kern_ms, "window_batch256", taps, local_rank)
     # e2e through the server's host path: one batch of host requests
     e2e = None
     if not args.no_e2e:
@@ -795,7 +835,7 @@ def run_single(args, rank, world, local_rank, dist):
                      "gridding_kernel": round(mean_kern, 4)},
         "accuracy": err, "flags": flags,
         "roofline": roofline(f"{mode_name}_kernel", alg, mean_kern,
-                             f"{mode_name}_{args.workload}"),
+                             f"{mode_name}_{args.workload}", n * S * S, local_rank),
         "cpu_baseline": {"value": round(cv, 4), "unit": "Mvis/s", "cores": ct, "kind": "port",
                          "sample": f"first {cn} visibilities of the workload ({cs:.1f} s), "
                                    f"gridCPU_pz restatement over {ct} row bands"},

@@ -22,6 +22,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgg.so")
+# measurement helper of the benchmark (reduction-rate probe), a separate library
+PROBE_SRC = "gg_probe.cu"
+PROBE_LIB = os.path.join(HERE, "libgg_probe.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["gg_api.cu", "gg_bin.cu", "gg_scatter.cu", "gg_window.cu",
@@ -97,8 +100,19 @@ def build(force: bool = False, debug: bool = False, verbose: bool = False) -> st
         os.replace(LIB + ".tmp", LIB)
         with open(stamp, "w") as fh:
             fh.write(link_tag)
+    # the probe library
+    psrc = os.path.join(CSRC, PROBE_SRC)
+    ptag = _digest([psrc], " ".join(flags))
+    pobj = os.path.join(BUILD, f"gg_probe.{ptag}.o")
+    if force or not os.path.exists(pobj) or not os.path.exists(PROBE_LIB):
+        compile_one((psrc, pobj))
+        cmd = [nv, "-shared", "-o", PROBE_LIB + ".tmp", pobj] + ARCH + ["-cudart", "shared"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(PROBE_LIB + ".tmp", PROBE_LIB)
     # drop stale objects of earlier source versions
-    keep = set(objs)
+    keep = set(objs) | {pobj}
     for f in os.listdir(BUILD):
         p = os.path.join(BUILD, f)
         if f.endswith(".o") and p not in keep:
