@@ -317,7 +317,7 @@ def run_served(args, rank, world, local_rank, dist):
     total_vis = int(specs["nvis"].sum())
     dp = DevicePools(pools, dev)
     opts = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
-                      layout=gg.LAYOUT_INTERLEAVED)
+                      layout=gg.LAYOUT_INTERLEAVED, autotune=True)
     srv = gg.Server(device=local_rank, streams=w["streams"], max_batch_jobs=w["max_batch_jobs"],
                     max_batch_vis=w["max_batch_vis"], hbm_budget=w["budget"], options=opts)
     gids = {S: srv.add_gcf(gcfs[S]) for S in (8, 16)}
@@ -403,7 +403,9 @@ def run_served(args, rank, world, local_rank, dist):
     for label, o in (("plain_scatter_per_request",
                       gg.Options(mode=gg.MODE_SCATTER, accum=gg.ACC_PLAIN,
                                  layout=gg.LAYOUT_INTERLEAVED)),
-                     ("window_per_request", opts)):
+                     ("window_per_request",
+                      gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
+                                 layout=gg.LAYOUT_INTERLEAVED))):
         jobs = []
         for i in range(n):
             N, S = int(specs["side"][i]), int(specs["S"][i])
@@ -452,7 +454,12 @@ def run_served(args, rank, world, local_rank, dist):
         import torch as _t
         hp = {N: (_t.from_numpy(uv).pin_memory().numpy(), _t.from_numpy(v).pin_memory().numpy())
               for N, (uv, v) in pools.items()}
-        hout = {N: _t.empty(N * N, dtype=_t.complex64).pin_memory().numpy() for N in hp}
+        # the client: each finished grid is copied to one of RING pinned host
+        # buffers of its size on one of 4 client streams (asynchronously,
+        # overlapping the server's batches), and released once its copy is done
+        RING, INFLIGHT = 8, 48
+        hout = {N: [_t.empty(N * N, dtype=_t.complex64).pin_memory() for _ in range(RING)]
+                for N in hp}
         hreqs = []
         for i in range(n):
             N, S = int(specs["side"][i]), int(specs["S"][i])
@@ -463,26 +470,50 @@ def run_served(args, rank, world, local_rank, dist):
                                            vh.ctypes.data + (s_ * L + off) * 8, None, nv_, N, S,
                                            gids[S], flags=gg.REQ_KEEP_RESIDENT))
         cr = cudart()
+        cr.cudaMemcpyAsync.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                       ctypes.c_int, ctypes.c_void_p]
+        cr.cudaMemcpyAsync.restype = ctypes.c_int
+        client_streams = [torch.cuda.Stream() for _ in range(4)]
         t_all = 0.0
         for _ in range(max(1, min(args.steps, 3))):
             srv.stats(reset=True)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             tickets = srv.submit_schedule(hreqs, zeros)
+            slot_ev = {N: [None] * RING for N in hp}
+            used = {N: 0 for N in hp}
+            inflight = []
             for k, t in enumerate(tickets):
                 r = srv.wait(int(t), timeout=600)
                 N = int(specs["side"][k])
-                cr.cudaMemcpy(hout[N].ctypes.data, ctypes.c_void_p(r.device_out),
-                              hout[N].nbytes, 2)
-                srv.release(int(t))
+                i = used[N] % RING
+                used[N] += 1
+                if slot_ev[N][i] is not None:
+                    slot_ev[N][i].synchronize()
+                buf = hout[N][i]
+                cs = client_streams[k % len(client_streams)]
+                assert cr.cudaMemcpyAsync(buf.data_ptr(), ctypes.c_void_p(r.device_out),
+                                          buf.numel() * 8, 2, ctypes.c_void_p(cs.cuda_stream)) == 0
+                ev = torch.cuda.Event()
+                ev.record(cs)
+                slot_ev[N][i] = ev
+                inflight.append((int(t), ev))
+                while len(inflight) > INFLIGHT:
+                    tt, ee = inflight.pop(0)
+                    ee.synchronize()
+                    srv.release(tt)
+            for tt, ee in inflight:
+                ee.synchronize()
+                srv.release(tt)
             t_all += time.perf_counter() - t0
         reps = max(1, min(args.steps, 3))
         e2e = {"value": round(world * total_vis * reps / t_all / 1e6, 3), "unit": "Mvis/s",
                "h2d_bytes_per_step": int(total_vis * 24),
                "d2h_bytes_per_step": int(sum(8 * int(N) * int(N) for N in specs["side"])),
                "ms_per_step": round(1e3 * t_all / reps, 3),
-               "api": "gg_server_* (C ABI): inputs from pinned host memory, each grid "
-                      "copied back to the host"}
+               "api": "gg_server_* (C ABI): inputs from pinned host memory (copied by "
+                      "the server), each grid copied back to pinned host memory by the "
+                      "client as it completes"}
     srv.close()
 
     if rank != 0:
@@ -507,6 +538,7 @@ def run_served(args, rank, world, local_rank, dist):
                    "l2": "inputs (3.2 GB of track pools) exceed L2",
                    "timing": "server clock from first arrival to last grid ready, "
                              "per pass; device synchronised around the passes",
+                   "autotune": gg.autotune_report().splitlines(),
                    "parallelism": f"replicas x{world}"},
         "plain_per_request_Mvis_per_s": plain,
         "speedup_vs_best_plain": round(value / world / best_plain, 2),
@@ -540,7 +572,7 @@ def run_batch(args, rank, world, local_rank, dist):
     dp = DevicePools(pools, dev)
     dg = {S: torch.from_numpy(gcfs[S].reshape(-1)).to(dev) for S in (8, 16)}
     opts = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
-                      layout=gg.LAYOUT_INTERLEAVED)
+                      layout=gg.LAYOUT_INTERLEAVED, autotune=True)
     outs, jobs = [], []
     for i in range(n):
         N, S = int(specs["side"][i]), int(specs["S"][i])
@@ -603,7 +635,9 @@ def run_batch(args, rank, world, local_rank, dist):
     for label, o in (("plain_scatter_per_job",
                       gg.Options(mode=gg.MODE_SCATTER, accum=gg.ACC_PLAIN,
                                  layout=gg.LAYOUT_INTERLEAVED)),
-                     ("window_per_job", opts)):
+                     ("window_per_job",
+                      gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
+                                 layout=gg.LAYOUT_INTERLEAVED))):
         for j in jobs[:20]:
             ctx.grid_job(o, j)
         torch.cuda.synchronize()
@@ -628,7 +662,9 @@ def run_batch(args, rank, world, local_rank, dist):
               for N, (uv, v) in pools.items()}
         houts = [torch.empty(int(N) * int(N), dtype=torch.complex64).pin_memory().numpy()
                  for N in specs["side"]]
-        srv = gg.Server(device=local_rank, streams=1, max_batch_jobs=n, options=opts)
+        # host path: 3 stream slots, batches of up to 64 jobs, so that copies of
+        # one batch overlap the gridding of another
+        srv = gg.Server(device=local_rank, streams=3, max_batch_jobs=64, options=opts)
         gids = {S: srv.add_gcf(gcfs[S]) for S in (8, 16)}
         reqs = []
         for i in range(n):
@@ -656,7 +692,8 @@ def run_batch(args, rank, world, local_rank, dist):
                "h2d_bytes_per_step": int(total_vis * 24),
                "d2h_bytes_per_step": int(sum(8 * int(N) * int(N) for N in specs["side"])),
                "ms_per_step": round(1e3 * t_all / reps, 3),
-               "api": "gg_server_* (C ABI) with host input and output buffers"}
+               "api": "gg_server_* (C ABI) with host input and output buffers (3 stream "
+                      "slots, batches of up to 64 jobs)"}
     if rank != 0:
         return None
     cpu_jobs = []
@@ -675,6 +712,7 @@ def run_batch(args, rank, world, local_rank, dist):
                    "visibilities_per_step": total_vis, "jobs": n,
                    "l2": "flushed before every timed step (256 MiB write)",
                    "launch": "one gg_plan_launch captured in a CUDA graph, replayed",
+                   "autotune": gg.autotune_report().splitlines(),
                    "parallelism": f"replicas x{world}"},
         "plain_per_job_Mvis_per_s": plain,
         "speedup_vs_best_plain": round(value / world / max(plain.values()), 2),

@@ -86,7 +86,12 @@ typedef struct gg_options {
   int32_t window_chunk;  /* max visibilities per work item (0 -> default)    */
   int32_t group_warps;   /* moving window: warps sharing one sub-grid
                             (1, 2, 4 or 8; 0 -> chosen by support)           */
-  int32_t reserved[6];
+  int32_t autotune;      /* moving window with tile, group_warps and
+                            window_chunk all 0: 1 = pick them per support
+                            class by timing candidates on the first batch of
+                            each size class (that call synchronises its
+                            stream), then reuse the choice (process-wide)   */
+  int32_t reserved[5];
 } gg_options;
 
 /* Defaults = the reference built with no Makefile switches: SCATTER,
@@ -96,6 +101,11 @@ int gg_default_options(gg_options *opt);
 /* Process-wide options used by the drop-in gridGPU entry points below, the
  * run-time counterpart of Defines.h / Makefile switches. */
 int gg_set_global_options(const gg_options *opt);
+
+/* Autotuner cache (see gg_options.autotune): forget every choice, or write a
+ * text table of the choices made so far into buf (always NUL-terminated). */
+int gg_autotune_clear(void);
+int gg_autotune_report(char *buf, size_t len);
 int gg_get_global_options(gg_options *opt);
 
 const char *gg_last_error(void);

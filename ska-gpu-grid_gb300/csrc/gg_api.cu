@@ -14,8 +14,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -184,6 +186,7 @@ struct Plan {
     int S, j0, j1;
     int64_t v0, v1;  // global vis range
     int t0, t1;      // global tile range
+    int T, W, chunk; // tile, warps per sub-grid group (0: by support), records per item
   };
   std::vector<ClassRange> classes;
   std::vector<JobDesc> hjobs;
@@ -270,10 +273,84 @@ static int resolve_mode(const gg_options *o, int S) {
   return GG_MODE_WINDOW;  // measured fastest at every size class so far
 }
 
+// Launch configuration of one support class of the moving window
+struct ClassCfg {
+  int T = 0, W = 0, chunk = 0;
+};
+using ClassCfgs = std::map<int, ClassCfg>;  // by support
+
+// Autotuner cache: the configuration picked for a size class, keyed by
+// support, arithmetic, polarisations, oversampling and the class's density
+// (visibilities per 256 grid cells, as a power of two)
+struct TuneKey {
+  int S, accum, vals_f64, gauss, P, G, density;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(S, accum, vals_f64, gauss, P, G, density) <
+           std::tie(o.S, o.accum, o.vals_f64, o.gauss, o.P, o.G, o.density);
+  }
+};
+struct TuneEntry {
+  ClassCfg cfg;
+  double ms_best = 0, ms_default = 0;
+  int trials = 0;
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, TuneEntry> g_tune;
+
+static bool tunable(const gg_options *o) {
+  return o->tile == 0 && o->group_warps == 0 && o->window_chunk == 0;
+}
+
+// density class of the jobs of support S in a batch
+static int density_class(const gg_job *jobs, int njobs, int S) {
+  double vis = 0, area = 0;
+  for (int j = 0; j < njobs; ++j)
+    if (jobs[j].gcf_dim == S) {
+      vis += (double)jobs[j].npts;
+      area += (double)jobs[j].img_dim * (double)jobs[j].img_dim;
+    }
+  const double d = area > 0 ? vis * 256.0 / area : 0.0;
+  int b = 0;
+  while (b < 24 && d >= (double)(2ll << b)) ++b;
+  return b;
+}
+
+static TuneKey tune_key(const gg_options *o, int vals_f64, int S, int density) {
+  return {S, vals_f64 ? GG_ACC_PLAIN : o->accum, vals_f64, o->gcf_kind == GG_GCF_GAUSSIAN,
+          o->polarizations, o->oversample, density};
+}
+
+// classes smaller than this are not timed when a choice for the same support
+// and arithmetic exists (their trials are short and noisy); they take the
+// choice of the nearest density instead
+constexpr double kTuneMinVis = 1 << 23;
+
+// the cached entry of `k`, or of the nearest density with the same other
+// fields; null when there is none (caller holds g_tune_mu)
+static const TuneEntry *tune_lookup(const TuneKey &k) {
+  auto it = g_tune.find(k);
+  if (it != g_tune.end()) return &it->second;
+  const TuneEntry *best = nullptr;
+  int dist = 1 << 30;
+  for (const auto &kv : g_tune) {
+    const TuneKey &o = kv.first;
+    if (o.S != k.S || o.accum != k.accum || o.vals_f64 != k.vals_f64 || o.gauss != k.gauss ||
+        o.P != k.P || o.G != k.G)
+      continue;
+    const int d = std::abs(o.density - k.density);
+    if (d < dist) {
+      dist = d;
+      best = &kv.second;
+    }
+  }
+  return best;
+}
+
 // Build the plan for a batch: validate, resolve, order jobs by support class,
-// lay out the workspace.  No device work.
+// lay out the workspace.  No device work.  `force` fixes the configuration of
+// support classes (autotuner trials).
 static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
-                      int njobs, Plan &pl) {
+                      int njobs, Plan &pl, const ClassCfgs *force = nullptr) {
   int st = check_options(opt);
   if (st) return st;
   if (njobs < 1) return fail(GG_ERR_ARG, "no jobs");
@@ -281,18 +358,40 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
   pl = Plan();
   pl.G = opt->oversample;
   pl.P = opt->polarizations;
+  // per support class: tile, warps per sub-grid group, records per work item
+  ClassCfgs cfgs;
   {
-    // automatic tile: the moving window keeps one (T+S-1)^2 sub-grid per warp
-    // group, so small supports use 16-cell tiles; gather needs 32
     int64_t maxS = 0;
     for (int j = 0; j < njobs; ++j) maxS = std::max<int64_t>(maxS, jobs[j].gcf_dim);
     const int m0 = resolve_mode(opt, (int)maxS);
-    // (input declared tile-sorted: the caller's tiles are the default 32)
-    pl.T = opt->tile > 0 ? opt->tile
-                         : (m0 == GG_MODE_WINDOW && maxS <= 16 && !opt->input_sorted ? 16 : 32);
+    const int vf64 = jobs[0].vals_type == GG_C128;
+    for (int j = 0; j < njobs; ++j) {
+      const int S = (int)jobs[j].gcf_dim;
+      if (cfgs.count(S)) continue;
+      // automatic tile: the moving window keeps one (T+S-1)^2 sub-grid per
+      // warp group, so supports up to 16 use 16-cell tiles; gather needs 32;
+      // input declared tile-sorted: the caller's tiles are the default 32
+      ClassCfg cf;
+      cf.T = opt->tile > 0 ? opt->tile
+                           : (m0 == GG_MODE_WINDOW && S <= 16 && !opt->input_sorted ? 16 : 32);
+      cf.W = opt->group_warps;
+      cf.chunk = opt->window_chunk > 0 ? opt->window_chunk : 2048;
+      if (m0 == GG_MODE_WINDOW && tunable(opt)) {
+        if (force && force->count(S)) {
+          cf = force->at(S);
+        } else if (opt->autotune) {
+          std::lock_guard<std::mutex> lk(g_tune_mu);
+          const TuneEntry *e = tune_lookup(tune_key(opt, vf64, S, density_class(jobs, njobs, S)));
+          if (e) cf = e->cfg;
+        }
+      }
+      cfgs[S] = cf;
+    }
+    pl.T = cfgs.begin()->second.T;
+    pl.chunk = cfgs.begin()->second.chunk;
+    for (auto &kv : cfgs) pl.chunk = std::min(pl.chunk, kv.second.chunk);
+    pl.group_warps = opt->group_warps;
   }
-  pl.chunk = opt->window_chunk > 0 ? opt->window_chunk : 2048;
-  pl.group_warps = opt->group_warps;
   pl.input_sorted = opt->input_sorted ? 1 : 0;
   pl.gauss = opt->gcf_kind == GG_GCF_GAUSSIAN;
   pl.accum = opt->accum;
@@ -348,10 +447,11 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
       if (J.gcf_dim != jobs[order[0]].gcf_dim)
         return fail(GG_ERR_ARG, "on-the-fly GCF needs one support per batch");
     }
-    if (mode == GG_MODE_GATHER && pl.T != 32)
+    const int T = cfgs[(int)J.gcf_dim].T;
+    if (mode == GG_MODE_GATHER && T != 32)
       return fail(GG_ERR_ARG, "gather needs tile 32");
     vis += J.npts;
-    int ntx = (int)((J.img_dim + pl.T - 1) / pl.T);
+    int ntx = (int)((J.img_dim + T - 1) / T);
     tiles += (int64_t)ntx * ntx;
   }
   if (vis >= (1ll << 31) - 1024) return fail(GG_ERR_ARG, "batch has >= 2^31 visibilities");
@@ -359,14 +459,14 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
   pl.mode = mode;
   if (mode == GG_MODE_WINDOW) {
     for (int j = 0; j < njobs; ++j) {
+      const ClassCfg &cf = cfgs[(int)jobs[j].gcf_dim];
       const size_t need = window_smem_bytes((int)jobs[j].gcf_dim, opt->accum, vt == GG_C128,
-                                            pl.T, pl.group_warps,
-                                            opt->gcf_kind == GG_GCF_GAUSSIAN);
+                                            cf.T, cf.W, opt->gcf_kind == GG_GCF_GAUSSIAN);
       if (need > 227 * 1024)
         return fail(GG_ERR_ARG,
                     "tile %d with support %lld needs %zu bytes of shared memory "
                     "(max 232448): use a smaller tile",
-                    pl.T, (long long)jobs[j].gcf_dim, need);
+                    cf.T, (long long)jobs[j].gcf_dim, need);
     }
   }
   pl.sigma = (float)(sigma > 0 ? sigma : 0.0);
@@ -451,10 +551,12 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
         pl.classes.back().v1 = vb;
         pl.classes.back().t1 = tb;
       }
-      pl.classes.push_back({S, k, k, vb, vb, tb, tb});
+      const ClassCfg &cf = cfgs[S];
+      pl.classes.push_back({S, k, k, vb, vb, tb, tb, cf.T, cf.W, cf.chunk});
     }
+    const int T = pl.classes.back().T;
     const int N = (int)J.img_dim;
-    const int ntx = (N + pl.T - 1) / pl.T;
+    const int ntx = (N + T - 1) / T;
     JobDesc &D = pl.hjobs[k];
     memset(&D, 0, sizeof D);
     D.out = J.out;
@@ -468,8 +570,8 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
     D.G = pl.G;
     D.log2G = ilog2(pl.G);
     D.P = pl.P;
-    D.T = pl.T;
-    D.log2T = ilog2(pl.T);
+    D.T = T;
+    D.log2T = ilog2(T);
     D.ntx = ntx;
     int layout = opt->layout;
     if (layout == GG_LAYOUT_REFERENCE)
@@ -639,14 +741,19 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
   if (pl.mode == GG_MODE_WINDOW) {
     GG_CUDA(cudaMemsetAsync(flags + 8, 0, 8 * sizeof(int), s));
     WorkItem *items = (WorkItem *)(ws + pl.o_items);
+    ClassChunks chunks;
+    for (int ci = 0; ci < kMaxClasses; ++ci)
+      chunks.c[ci] = ci < (int)pl.classes.size() ? pl.classes[ci].chunk : pl.chunk;
     GG_CUDA(launch_make_items((const int *)(ws + pl.o_bm), dtileb, dclass, pl.njobs,
-                              pl.total_tiles, pl.chunk, items, pl.class_cap, flags + 8, s));
+                              pl.total_tiles, chunks, items, pl.class_cap, flags + 8, s));
     if (prof) GG_CUDA(cudaEventRecord(prof->ev[1], s));
     for (size_t ci = 0; ci < pl.classes.size(); ++ci) {
       const auto &cl = pl.classes[ci];
       g.jobs = djobs;
       g.njobs = pl.njobs;
       g.S = cl.S;
+      g.tile = cl.T;
+      g.group_warps = cl.W;
       g.items = items + ci * pl.class_cap;
       g.nitems = flags + 8 + ci;
       g.item_next = flags + 12 + ci;
@@ -688,11 +795,10 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
   return GG_OK;
 }
 
-static int grid_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs,
-                     int njobs, cudaStream_t s) {
-  GG_CUDA(cudaSetDevice(c->device));
+static int enqueue_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs,
+                        int njobs, cudaStream_t s, const ClassCfgs *force) {
   Plan &pl = c->plan;
-  int st = plan_build(c, opt, jobs, njobs, pl);
+  int st = plan_build(c, opt, jobs, njobs, pl, force);
   if (st) return st;
   // the workspace may be reallocated: earlier work on it must be finished
   if (pl.ws_bytes > c->ws.n) GG_CUDA(cudaEventSynchronize(c->exec_done));
@@ -710,6 +816,120 @@ static int grid_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs,
   if (c->profile) c->prof_recorded = 1;
   GG_CUDA(cudaEventRecord(c->exec_done, s));
   return GG_OK;
+}
+
+// Autotuner.  For every support class of a moving-window batch whose size
+// class has no entry yet, time candidate configurations on the class's own
+// jobs (coordinate descent: warps per sub-grid group, then tile, then records
+// per work item; two launches each, the faster counted) and record the
+// fastest.  The trials write the jobs' outputs, which the real launch then
+// overwrites; they synchronise stream s.
+static int autotune_batch(gg_context *c, const gg_options *opt, const gg_job *jobs, int njobs,
+                          cudaStream_t s) {
+  if (!opt->autotune || !tunable(opt) || njobs < 1 || !jobs) return GG_OK;
+  int maxS = 0;
+  for (int j = 0; j < njobs; ++j) maxS = std::max<int>(maxS, (int)jobs[j].gcf_dim);
+  if (resolve_mode(opt, maxS) != GG_MODE_WINDOW) return GG_OK;
+  const int vf64 = jobs[0].vals_type == GG_C128;
+  cudaEvent_t e0, e1;
+  GG_CUDA(cudaEventCreate(&e0));
+  GG_CUDA(cudaEventCreate(&e1));
+  int st = GG_OK;
+  std::vector<int> supports;
+  for (int j = 0; j < njobs; ++j)
+    if (std::find(supports.begin(), supports.end(), (int)jobs[j].gcf_dim) == supports.end())
+      supports.push_back((int)jobs[j].gcf_dim);
+  for (int S : supports) {
+    const TuneKey key = tune_key(opt, vf64, S, density_class(jobs, njobs, S));
+    std::vector<gg_job> sub;
+    double vis = 0;
+    for (int j = 0; j < njobs; ++j)
+      if (jobs[j].gcf_dim == S) {
+        sub.push_back(jobs[j]);
+        vis += (double)jobs[j].npts;
+      }
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      if (g_tune.count(key)) continue;
+      if (vis < kTuneMinVis && tune_lookup(key)) continue;
+    }
+    int trials = 0;
+    // time one configuration; a configuration the plan rejects (shared
+    // memory) counts as infinitely slow
+    auto timeit = [&](const ClassCfg &cf) -> double {
+      ClassCfgs f{{S, cf}};
+      double best = 1e30;
+      for (int rep = 0; rep < 2; ++rep) {
+        if (cudaEventRecord(e0, s) != cudaSuccess) return 1e30;
+        if (enqueue_jobs(c, opt, sub.data(), (int)sub.size(), s, &f) != GG_OK) return 1e30;
+        float ms = 0.f;
+        if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+          return 1e30;
+        best = std::min(best, (double)ms);
+      }
+      ++trials;
+      return best;
+    };
+    ClassCfg base;
+    base.T = S <= 16 && !opt->input_sorted ? 16 : 32;
+    base.W = 0;
+    base.chunk = 2048;
+    const double t_default = timeit(base);
+    if (t_default >= 1e30) {
+      st = fail(GG_ERR_CUDA, "autotune: the default configuration failed for support %d", S);
+      break;
+    }
+    ClassCfg best = base;
+    double t_best = t_default;
+    auto consider = [&](ClassCfg cf) {
+      const double t = timeit(cf);
+      if (t < t_best) {
+        t_best = t;
+        best = cf;
+      }
+    };
+    static const int kWarps[] = {1, 2, 4, 8};
+    for (int w : kWarps) {
+      if ((S == 4 && w != 1) || (S == 8 && w > 2) || (S == 16 && w > 4) || (S == 32 && w < 4))
+        continue;
+      ClassCfg cf = best;
+      cf.W = w;
+      consider(cf);
+    }
+    if (!opt->input_sorted)
+      for (int T : {16, 32}) {
+        if (T == best.T) continue;
+        ClassCfg cf = best;
+        cf.T = T;
+        consider(cf);
+      }
+    for (int ch : {1024, 4096}) {
+      ClassCfg cf = best;
+      cf.chunk = ch;
+      consider(cf);
+    }
+    // a rejected trial configuration leaves its message: clear it
+    g_last_error.clear();
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    TuneEntry &e = g_tune[key];
+    e.cfg = best;
+    e.ms_best = t_best;
+    e.ms_default = t_default;
+    e.trials = trials;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return st;
+}
+
+static int grid_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs,
+                     int njobs, cudaStream_t s) {
+  GG_CUDA(cudaSetDevice(c->device));
+  int st = check_options(opt);
+  if (st) return st;
+  if ((st = autotune_batch(c, opt, jobs, njobs, s))) return st;
+  return enqueue_jobs(c, opt, jobs, njobs, s, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -736,6 +956,31 @@ int gg_get_global_options(gg_options *opt) {
   if (!opt) return fail(GG_ERR_ARG, "opt: null");
   std::lock_guard<std::mutex> lk(g_opt_mu);
   *opt = g_global_opts;
+  return GG_OK;
+}
+
+int gg_autotune_clear(void) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+  return GG_OK;
+}
+
+int gg_autotune_report(char *buf, size_t len) {
+  if (!buf || len == 0) return fail(GG_ERR_ARG, "buf: null or empty");
+  std::string r;
+  char line[256];
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (const auto &kv : g_tune) {
+    const TuneKey &k = kv.first;
+    const TuneEntry &e = kv.second;
+    snprintf(line, sizeof line,
+             "support %d accum %d f64 %d gauss %d pols %d G %d density 2^%d vis/256 cells: "
+             "tile %d group_warps %d chunk %d (%.3f ms; default %.3f ms; %d trials)\n",
+             k.S, k.accum, k.vals_f64, k.gauss, k.P, k.G, k.density, e.cfg.T, e.cfg.W,
+             e.cfg.chunk, e.ms_best, e.ms_default, e.trials);
+    r += line;
+  }
+  snprintf(buf, len, "%s", r.c_str());
   return GG_OK;
 }
 
@@ -843,8 +1088,13 @@ int gg_plan_create(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
   std::unique_ptr<gg_plan> p(new (std::nothrow) gg_plan);
   if (!p) return fail(GG_ERR_NOMEM, "plan allocation");
   p->ctx = ctx;
+  if (!opt) return fail(GG_ERR_ARG, "opt: null");
   p->opt = *opt;
-  int st = plan_build(ctx, opt, jobs, njobs, p->pl);
+  int st = check_options(opt);
+  if (st) return st;
+  if ((st = autotune_batch(ctx, opt, jobs, njobs, ctx->own))) return st;
+  GG_CUDA(cudaStreamSynchronize(ctx->own));
+  st = plan_build(ctx, opt, jobs, njobs, p->pl);
   if (st) return st;
   if ((st = p->ws.ensure(p->pl.ws_bytes))) return st;
   if ((st = p->flags.ensure(64 * sizeof(int)))) {

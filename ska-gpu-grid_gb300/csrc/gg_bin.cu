@@ -308,23 +308,23 @@ cudaError_t run_binning(const BinBuffers &b, cudaStream_t s) {
 }
 
 // ---- work items ---------------------------------------------------------------
-constexpr int kMaxClasses = 4;
 
 __global__ void __launch_bounds__(256)
     make_items_kernel(const int *bm, const int *tile_base, const int *job_class,
-                      int njobs, int total_tiles, int chunk, WorkItem *items,
+                      int njobs, int total_tiles, ClassChunks chunks, WorkItem *items,
                       int64_t class_cap, int *counters) {
   const int lane = threadIdx.x & 31;
   for (int base = blockIdx.x * 256 + (threadIdx.x & ~31); base < total_tiles;
        base += gridDim.x * 256) {
     int t = base + lane;
-    int k = 0, s0 = 0, e0 = 0, j = 0, cls = 0;
+    int k = 0, s0 = 0, e0 = 0, j = 0, cls = 0, chunk = 1;
     if (t < total_tiles) {
       s0 = bm[t];
       e0 = bm[t + 1];
-      k = (e0 - s0 + chunk - 1) / chunk;
       j = njobs == 1 ? 0 : find_job32(tile_base, njobs, t);
       cls = job_class ? job_class[j] : 0;
+      chunk = chunks.c[cls];
+      k = (e0 - s0 + chunk - 1) / chunk;
     }
 #pragma unroll
     for (int c = 0; c < kMaxClasses; ++c) {
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(256)
 
 cudaError_t launch_make_items(const int *bookmarks, const int *tile_base,
                               const int *job_class, int njobs, int total_tiles,
-                              int chunk, WorkItem *items, int64_t class_cap,
+                              ClassChunks chunk, WorkItem *items, int64_t class_cap,
                               int *counters, cudaStream_t s) {
   if (total_tiles <= 0) return cudaSuccess;
   make_items_kernel<<<grid_for(total_tiles), 256, 0, s>>>(

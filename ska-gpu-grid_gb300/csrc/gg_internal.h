@@ -62,11 +62,15 @@ cudaError_t scan_exclusive(int *data, int64_t n, int *tmp, cudaStream_t s);
 // (global tiles tile_base..) is cut into slices of at most `chunk` sorted
 // visibilities.  Items of jobs of S-class c go to items + c*class_cap,
 // counted in counters[c].
+// records per work item of each support class (index: class of the job)
+constexpr int kMaxClasses = 4;
+struct ClassChunks {
+  int c[kMaxClasses];
+};
 cudaError_t launch_make_items(const int *bookmarks, const int *tile_base,
-                              const int *job_class, int njobs,
-                              int total_tiles, int chunk, WorkItem *items,
-                              int64_t class_cap, int *counters,
-                              cudaStream_t s);
+                              const int *job_class, int njobs, int total_tiles,
+                              ClassChunks chunk, WorkItem *items, int64_t class_cap,
+                              int *counters, cudaStream_t s);
 
 // ---- gridding launches ----------------------------------------------------
 struct GridLaunch {

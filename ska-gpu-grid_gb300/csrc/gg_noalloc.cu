@@ -232,8 +232,9 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   GG_NA(run_binning(b, s));
 
   WorkItem *items = (WorkItem *)(ws + kOffItems);
+  const ClassChunks chunks = {{kNoAllocChunk, kNoAllocChunk, kNoAllocChunk, kNoAllocChunk}};
   GG_NA(launch_make_items(b.bookmarks, b.tile_base, (const int *)(ws + kOffClass), 1,
-                          b.total_tiles, kNoAllocChunk, items, kClassCap, flags + 8, s));
+                          b.total_tiles, chunks, items, kClassCap, flags + 8, s));
   GridLaunch g{};
   g.jobs = (const JobDesc *)(ws + kOffJobs);
   g.njobs = 1;

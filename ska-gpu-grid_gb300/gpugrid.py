@@ -55,7 +55,8 @@ class gg_options(ctypes.Structure):
                 ("gcf_sigma", ctypes.c_double),
                 ("window_chunk", ctypes.c_int32),
                 ("group_warps", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 6)]
+                ("autotune", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
 
 
 class gg_job(ctypes.Structure):
@@ -152,6 +153,8 @@ def _load():
         "gg_server_get_stats": ([vp, P(gg_server_stats), ctypes.c_int], ctypes.c_int),
         "gg_server_drain": ([vp, ctypes.c_double], ctypes.c_int),
         "gg_server_destroy": ([vp], ctypes.c_int),
+        "gg_autotune_clear": ([], ctypes.c_int),
+        "gg_autotune_report": ([ctypes.c_char_p, sz], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -182,6 +185,7 @@ class Options:
     gcf_sigma: float = 0.0
     window_chunk: int = 0
     group_warps: int = 0                # moving window: warps per sub-grid
+    autotune: bool = False              # moving window: tile / warps / chunk by timing
 
     def c(self) -> gg_options:
         o = gg_options()
@@ -192,6 +196,7 @@ class Options:
         o.input_sorted = int(bool(self.input_sorted))
         o.gcf_sigma, o.window_chunk = self.gcf_sigma, self.window_chunk
         o.group_warps = self.group_warps
+        o.autotune = int(bool(self.autotune))
         return o
 
 
@@ -506,6 +511,17 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def autotune_report() -> str:
+    """the autotuner's choices so far, one line per size class"""
+    buf = ctypes.create_string_buffer(1 << 16)
+    _check(LIB.gg_autotune_report(buf, len(buf)))
+    return buf.value.decode()
+
+
+def autotune_clear() -> None:
+    _check(LIB.gg_autotune_clear())
 
 
 def kernel_launches() -> int:

@@ -290,14 +290,17 @@ def test_batch_equals_single_jobs(ctx, mode):
         assert rel_err(out, ref) <= TOL["cc_comp"]
 
 
-@pytest.mark.parametrize("accum", ["cc_comp", "cc"])
-def test_batch_of_track_jobs_matches_oracle(ctx, accum):
+@pytest.mark.parametrize("accum,autotune", [("cc_comp", False), ("cc", False),
+                                            ("cc_comp", True)])
+def test_batch_of_track_jobs_matches_oracle(ctx, accum, autotune):
     """Batched moving-window gridding of dense uv-track jobs (whole baseline
     tracks at 2080 samples over +-4 h, several grid sides and both supports,
     one job overfilling its grid so that edge tiles hold clamped mains):
     every job against the oracle."""
     rng = np.random.default_rng(31)
-    o = opts_for("window", accum, layout=gg.LAYOUT_INTERLEAVED)
+    o = opts_for("window", accum, layout=gg.LAYOUT_INTERLEAVED, autotune=autotune)
+    if autotune:
+        gg.autotune_clear()
     specs = [(256, 8, 1.0), (256, 16, 0.9), (512, 8, 0.9), (512, 16, 1.05),
              (1024, 8, 0.9), (1024, 16, 0.9), (128, 16, 1.2), (512, 8, 0.6)]
     jobs, keep, refs = [], [], []
@@ -313,13 +316,20 @@ def test_batch_of_track_jobs_matches_oracle(ctx, accum):
         keep.append(d)
         jobs.append(gg.Context.make_job(d[3], d[0], d[1], d[2], N, S))
         refs.append(oracle_for(uv, vals, gcf, N, S))
-    for rep in range(2):  # the second launch reuses the workspace
+    for rep in range(2):  # the second launch reuses the workspace (and the tuning)
         ctx.grid_batch(o, jobs)
         torch.cuda.synchronize()
         assert ctx.read_flags() == [0, 0, 0, 0]
         for (N, S, _), d, ref in zip(specs, keep, refs):
             host = torch.view_as_real(d[3]).reshape(-1).cpu().numpy()
             assert rel_err(planar_from_grid(host, 1, N, False), ref) <= TOL[accum], (N, S, rep)
+        if autotune:
+            report = gg.autotune_report()
+            if rep == 0:
+                first = report
+            # one entry per support class, chosen once
+            assert len(report.splitlines()) == 2 and report == first
+            assert "support 8 " in report and "support 16 " in report
 
 
 # ---------------------------------------------------------------------------
