@@ -87,7 +87,7 @@ WORKLOADS = {
               "FP64 scatter")),
     "disk8192": dict(
         kind="single", N=8192, S=32, npts=1 << 24, gen="disk", vals="c64", out="c128",
-        mode="auto", accum="comp", gcf="gauss",
+        mode="auto", accum="comp", gcf="gauss", precision_study=True,
         desc=("8192^2 grid (complex128 output of FP32 compensated "
               "accumulation); 2^24 visibilities, uniform disk; N(0,1) values "
               "with 1% outliers at 1e3; support 32, oversample 8; GCF computed "
@@ -784,17 +784,33 @@ def run_single(args, rank, world, local_rank, dist):
     flags = ctx.read_flags()
     err = None
     if rank == 0 and not args.no_check:
-        nchk = n if N <= 4096 else n // 16
-        if nchk < n:
-            ctx.grid(o, out, d_uv[:nchk], d_vals[:nchk], d_gcf, N, S)
+        nchk = n if (N <= 4096 or w.get("precision_study")) else n // 16
         ref = O.grid_pz(uv[:nchk], pairs(vals[:nchk]), pairs(gcf), N, S, nthreads=os.cpu_count())
-        got = torch.view_as_real(out).reshape(N, N, 2).cpu().numpy().astype(np.float64)
-        d = max(np.abs(got[..., 0] - ref[0, 0]).max(), np.abs(got[..., 1] - ref[1, 0]).max())
         den = max(np.abs(ref).max(), 1e-300)
-        rms = np.sqrt(((got[..., 0] - ref[0, 0]) ** 2 + (got[..., 1] - ref[1, 0]) ** 2).sum()
-                      / (ref ** 2).sum())
-        err = {"max_rel": float(d / den), "rms_rel": float(rms), "visibilities_checked": int(nchk)}
-        del ref, got
+        rden = np.sqrt((ref ** 2).sum())
+
+        def error_of(opts, grid=out):
+            ctx.grid(opts, grid, d_uv[:nchk], d_vals[:nchk], d_gcf, N, S)
+            got = torch.view_as_real(grid).reshape(N, N, 2).cpu().numpy().astype(np.float64)
+            d = max(np.abs(got[..., 0] - ref[0, 0]).max(), np.abs(got[..., 1] - ref[1, 0]).max())
+            rms = np.sqrt(((got[..., 0] - ref[0, 0]) ** 2 + (got[..., 1] - ref[1, 0]) ** 2).sum())
+            return {"max_rel": float(d / den), "rms_rel": float(rms / rden)}
+
+        err = error_of(o)
+        err["visibilities_checked"] = int(nchk)
+        err["reference"] = "FP64 oracle (gridCPU_pz restatement)"
+        if w.get("precision_study") and w["vals"] == "c64":
+            # the precision form: the same visibilities with plain FP32 sums,
+            # into the workload's complex128 grid and into a complex64 grid
+            plain = single_options(dict(w, accum="plain"))
+            out64 = torch.empty(N * N, dtype=torch.complex64, device=dev)
+            err["by_accumulation"] = {
+                "complex128_grid": {"fp32_compensated": error_of(o),
+                                    "fp32_plain": error_of(plain)},
+                "complex64_grid": {"fp32_compensated": error_of(o, out64),
+                                   "fp32_plain": error_of(plain, out64)}}
+            del out64
+        del ref
     start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     kern_ms, bin_ms = [], []

@@ -101,12 +101,12 @@ int gg_default_options(gg_options *opt);
 /* Process-wide options used by the drop-in gridGPU entry points below, the
  * run-time counterpart of Defines.h / Makefile switches. */
 int gg_set_global_options(const gg_options *opt);
+int gg_get_global_options(gg_options *opt);
 
 /* Autotuner cache (see gg_options.autotune): forget every choice, or write a
  * text table of the choices made so far into buf (always NUL-terminated). */
 int gg_autotune_clear(void);
 int gg_autotune_report(char *buf, size_t len);
-int gg_get_global_options(gg_options *opt);
 
 const char *gg_last_error(void);
 int gg_abi_version(void);
@@ -158,7 +158,15 @@ typedef struct gg_job {
   int32_t uv_type, vals_type, out_type;
   int32_t reserved0;
   double gcf_sigma;   /* overrides options.gcf_sigma when > 0             */
-  int64_t reserved[4];
+  const int32_t *gcf_index; /* device, optional (TABLE GCF, scatter or moving
+                         window): per-visibility table index -- visibility n
+                         uses table gcf_index[n] of n_gcf consecutive
+                         [G*G][S][S] tables at gcf (a w-plane or baseline
+                         GCF, the reference's vis.gcfinx, vis.h:17);
+                         visibilities with an index outside [0, n_gcf) are
+                         dropped and counted like bad indices             */
+  int64_t n_gcf;      /* tables at gcf when gcf_index is set (1..32768)    */
+  int64_t reserved[2];
 } gg_job;
 
 /* Grid one job on `stream` (a cudaStream_t; NULL = the legacy default

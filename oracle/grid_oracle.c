@@ -28,6 +28,8 @@ typedef struct {
   size_t npts, img_dim, gcf_dim;
   int G, P, debug1;
   long y0, y1; /* rows owned by this worker: [y0, y1) */
+  const int32_t *gcfinx; /* per-visibility table index (NULL: table 0) */
+  int n_gcf;
 } band_job;
 
 /* Body of gridCPU_pz (grid.cu:157-191), restricted to rows [y0, y1).  The
@@ -47,7 +49,13 @@ static void grid_band(const band_job *j) {
     index_step(j->uv[2 * n + 1], G, &main_y, &sub_y);
     if ((long)main_y + S / 2 < j->y0 || (long)main_y - S / 2 + 1 >= j->y1)
       continue; /* footprint misses this band entirely */
-    const double *g = gcf + 2 * (S * S * ((long)G * sub_y + sub_x));
+    long table = 0;
+    if (j->gcfinx) {
+      /* vis.gcfinx (vis.h:17): the visibility's own [G*G][S][S] table */
+      if (j->gcfinx[n] < 0 || j->gcfinx[n] >= j->n_gcf) continue;
+      table = (long)j->gcfinx[n] * G * G * S * S;
+    }
+    const double *g = gcf + 2 * (table + S * S * ((long)G * sub_y + sub_x));
     for (long a = S / 2; a > -S / 2; a--)
       for (long b = S / 2; b > -S / 2; b--) {
         long x = main_x + a, y = main_y + b;
@@ -74,7 +82,7 @@ void oracle_grid_pz(double *out_planar, const double *uv, const double *vals,
                     size_t npts, size_t img_dim, const double *gcf,
                     size_t gcf_dim, int gcf_grid, int pols, int debug1) {
   band_job j = {out_planar, uv, vals, gcf, npts, img_dim, gcf_dim,
-                gcf_grid, pols, debug1, 0, (long)img_dim};
+                gcf_grid, pols, debug1, 0, (long)img_dim, NULL, 1};
   grid_band(&j);
 }
 
@@ -87,6 +95,15 @@ void oracle_grid_pz_mt(double *out_planar, const double *uv,
                        const double *vals, size_t npts, size_t img_dim,
                        const double *gcf, size_t gcf_dim, int gcf_grid,
                        int pols, int debug1, int nthreads) {
+  oracle_grid_pz_gcfinx(out_planar, uv, vals, NULL, npts, img_dim, gcf, 1,
+                        gcf_dim, gcf_grid, pols, debug1, nthreads);
+}
+
+void oracle_grid_pz_gcfinx(double *out_planar, const double *uv,
+                           const double *vals, const int32_t *gcfinx,
+                           size_t npts, size_t img_dim, const double *gcf,
+                           int n_gcf, size_t gcf_dim, int gcf_grid, int pols,
+                           int debug1, int nthreads) {
   if (nthreads < 1) nthreads = 1;
   if ((size_t)nthreads > img_dim) nthreads = (int)img_dim;
   band_job *jobs = (band_job *)calloc((size_t)nthreads, sizeof(band_job));
@@ -95,7 +112,8 @@ void oracle_grid_pz_mt(double *out_planar, const double *uv,
     band_job j = {out_planar, uv, vals, gcf, npts, img_dim, gcf_dim,
                   gcf_grid, pols, debug1,
                   (long)(img_dim * (size_t)t / (size_t)nthreads),
-                  (long)(img_dim * (size_t)(t + 1) / (size_t)nthreads)};
+                  (long)(img_dim * (size_t)(t + 1) / (size_t)nthreads),
+                  gcfinx, n_gcf};
     jobs[t] = j;
   }
   char *joined = (char *)calloc((size_t)nthreads, 1);

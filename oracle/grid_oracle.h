@@ -42,6 +42,17 @@ void oracle_grid_pz_mt(double *out_planar, const double *uv,
                        const double *gcf, size_t gcf_dim, int gcf_grid,
                        int pols, int debug1, int nthreads);
 
+/* gridCPU_pz with a table per visibility: visibility n reads table
+ * gcfinx[n] of n_gcf consecutive [G*G][S][S] tables -- the selection the
+ * reference's vis.gcfinx (vis.h:17, set per baseline in hdf52struct.cpp:116)
+ * stands for; its gridders themselves use one table.  A visibility whose
+ * index is outside [0, n_gcf) is skipped.  gcfinx NULL = table 0 for all. */
+void oracle_grid_pz_gcfinx(double *out_planar, const double *uv,
+                           const double *vals, const int32_t *gcfinx,
+                           size_t npts, size_t img_dim, const double *gcf,
+                           int n_gcf, size_t gcf_dim, int gcf_grid, int pols,
+                           int debug1, int nthreads);
+
 /* The index step of gridCPU_pz (grid.cu:159-163): main = floor(u),
  * sub = floorf(G*(u - floorf(u))) with the float conversions C applies.
  * Writes packed (main*G+sub) pairs like vis2ints (grid_gpu.cu:352-365). */

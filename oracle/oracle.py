@@ -50,6 +50,9 @@ def lib():
         L.oracle_grid_pz.argtypes = [_dp, _dp, _dp, _sz, _sz, _dp, _sz,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_grid_pz_mt.argtypes = L.oracle_grid_pz.argtypes + [ctypes.c_int]
+        L.oracle_grid_pz_gcfinx.argtypes = [_dp, _dp, _dp, _ip, _sz, _sz, _dp, ctypes.c_int,
+                                            _sz, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int]
         L.oracle_vis2ints.argtypes = [_dp, _sz, ctypes.c_int, _ip]
         L.oracle_vis2ints_gpu_formula.argtypes = [_dp, _sz, ctypes.c_int, _ip]
         L.oracle_set_bookmarks.argtypes = [_ip, _sz, ctypes.c_int, ctypes.c_int,
@@ -57,7 +60,8 @@ def lib():
         L.oracle_gaussian_gcf.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_double]
         L.oracle_gcf_from_1d.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int]
-        for f in (L.oracle_grid_pz, L.oracle_grid_pz_mt, L.oracle_vis2ints,
+        for f in (L.oracle_grid_pz, L.oracle_grid_pz_mt, L.oracle_grid_pz_gcfinx,
+                  L.oracle_vis2ints,
                   L.oracle_vis2ints_gpu_formula, L.oracle_set_bookmarks,
                   L.oracle_gaussian_gcf, L.oracle_gcf_from_1d):
             f.restype = None
@@ -93,6 +97,26 @@ def grid_pz(uv, vals, gcf, img_dim: int, gcf_dim: int, pols: int = 1,
         lib().oracle_grid_pz_mt(*args, nthreads)
     else:
         lib().oracle_grid_pz(*args)
+    return out
+
+
+def grid_pz_gcfinx(uv, vals, gcfinx, gcfs, img_dim: int, gcf_dim: int, pols: int = 1,
+                   gcf_grid: int = 8, nthreads: int = 1) -> np.ndarray:
+    """gridCPU_pz with a table per visibility: visibility n reads table
+    gcfinx[n] of the stack ``gcfs`` (n_gcf tables of G*G*S*S complex);
+    indices outside [0, n_gcf) are skipped.  Returns (2, P, N, N)."""
+    uv = _as_pairs(uv)
+    vals = _as_pairs(vals)
+    tabs = _as_pairs(gcfs)
+    per = gcf_grid * gcf_grid * gcf_dim * gcf_dim
+    assert tabs.shape[0] % per == 0
+    n_gcf = tabs.shape[0] // per
+    npts = uv.shape[0]
+    idx = np.ascontiguousarray(gcfinx, np.int32)
+    assert idx.shape == (npts,) and vals.shape[0] == npts * pols
+    out = np.zeros((2, pols, img_dim, img_dim), np.float64)
+    lib().oracle_grid_pz_gcfinx(_ptr(out), _ptr(uv), _ptr(vals), _ptr(idx, _ip), npts, img_dim,
+                                _ptr(tabs), n_gcf, gcf_dim, gcf_grid, pols, 0, max(1, nthreads))
     return out
 
 

@@ -203,6 +203,7 @@ struct Plan {
     const void *src;
     size_t off;
     int S;
+    int ntab;  // consecutive tables (per-visibility selection)
   };
   std::vector<GcfCopy> gcf_copies;
   std::vector<size_t> hgcf_off;
@@ -435,6 +436,14 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
       return fail(GG_ERR_ARG, "job %d: uv/vals null", j);
     if (opt->gcf_kind == GG_GCF_TABLE && !J.gcf)
       return fail(GG_ERR_ARG, "job %d: TABLE GCF needs gcf", j);
+    if (J.gcf_index) {
+      if (opt->gcf_kind != GG_GCF_TABLE)
+        return fail(GG_ERR_ARG, "job %d: gcf_index needs a TABLE GCF", j);
+      if (J.n_gcf < 1 || J.n_gcf > 32768)
+        return fail(GG_ERR_ARG, "job %d: n_gcf %lld outside 1..32768", j, (long long)J.n_gcf);
+      if (opt->input_sorted)
+        return fail(GG_ERR_ARG, "job %d: gcf_index with input_sorted is not supported", j);
+    }
     const int m = resolve_mode(opt, (int)J.gcf_dim);
     if (mode < 0) mode = m;
     if (m != mode) return fail(GG_ERR_ARG, "job %d: mixed methods in one batch", j);
@@ -450,9 +459,11 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
     const int T = cfgs[(int)J.gcf_dim].T;
     if (mode == GG_MODE_GATHER && T != 32)
       return fail(GG_ERR_ARG, "gather needs tile 32");
+    if (mode == GG_MODE_GATHER && J.gcf_index)
+      return fail(GG_ERR_ARG, "job %d: gcf_index: use the scatter or moving-window method", j);
     vis += J.npts;
     int ntx = (int)((J.img_dim + T - 1) / T);
-    tiles += (int64_t)ntx * ntx;
+    tiles += (int64_t)ntx * ntx * (J.gcf_index ? J.n_gcf : 1);
   }
   if (vis >= (1ll << 31) - 1024) return fail(GG_ERR_ARG, "batch has >= 2^31 visibilities");
   if (tiles >= (1ll << 30)) return fail(GG_ERR_ARG, "batch has too many uv tiles");
@@ -517,15 +528,16 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
   pl.gcf_copies.clear();
   pl.hgcf_off.assign(njobs, SIZE_MAX);
   if (mode == GG_MODE_WINDOW && !pl.gauss) {
-    std::map<std::pair<const void *, int>, size_t> seen;
+    std::map<std::tuple<const void *, int, int>, size_t> seen;
     for (int k = 0; k < njobs; ++k) {
       const gg_job &J = jobs[order[k]];
-      const std::pair<const void *, int> key(count ? nullptr : J.gcf, (int)J.gcf_dim);
+      const int ntab = J.gcf_index ? (int)J.n_gcf : 1;
+      const std::tuple<const void *, int, int> key(count ? nullptr : J.gcf, (int)J.gcf_dim, ntab);
       auto it = seen.find(key);
       if (it == seen.end()) {
-        const size_t o = take(gcf_double_rows_bytes(key.second, pl.G, (int)vbytes));
+        const size_t o = take(gcf_double_rows_bytes((int)J.gcf_dim, pl.G, (int)vbytes) * ntab);
         it = seen.emplace(key, o).first;
-        pl.gcf_copies.push_back({key.first, o, key.second});
+        pl.gcf_copies.push_back({std::get<0>(key), o, (int)J.gcf_dim, ntab});
       }
       pl.hgcf_off[k] = it->second;
     }
@@ -580,6 +592,8 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
     D.out_f64 = J.out_type == GG_C128;
     D.uv_f64 = J.uv_type == GG_C128;
     D.sigma = pl.sigma;
+    D.gcf_index = J.gcf_index;
+    D.n_gcf = J.gcf_index ? (int)J.n_gcf : 1;
     BinJob &B = pl.hbin[k];
     memset(&B, 0, sizeof B);
     B.uv = J.uv;
@@ -587,7 +601,9 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
     B.vis_base = vb;
     B.npts = J.npts;
     B.tile_base = tb;
-    B.ntiles = ntx * ntx;
+    B.ntiles = ntx * ntx * D.n_gcf;
+    B.gcf_index = J.gcf_index;
+    B.n_gcf = D.n_gcf;
     B.N = N;
     B.S = S;
     B.G = pl.G;
@@ -612,7 +628,7 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
       cnt_off += J.npts * pl.P;
     }
     vb += J.npts;
-    tb += ntx * ntx;
+    tb += ntx * ntx * D.n_gcf;
   }
   pl.classes.back().j1 = njobs;
   pl.classes.back().v1 = vb;
@@ -699,7 +715,7 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
   }
   for (const auto &c : pl.gcf_copies)
     GG_CUDA(launch_gcf_double_rows(c.src ? c.src : ws + pl.o_count_gcf, ws + c.off, c.S, pl.G,
-                                   (int)vbytes, s));
+                                   c.ntab, (int)vbytes, s));
 
   GridLaunch g{};
   g.accum = pl.accum;

@@ -99,6 +99,11 @@ __global__ void __launch_bounds__(256) bin_count_kernel(BinBuffers b) {
       bool ok = uv_index(J.uv, J.uv_f64, g - J.vis_base, J.G, mx, sx, my, sy);
       if (ok && ((unsigned)sx >= (unsigned)J.G || (unsigned)sy >= (unsigned)J.G))
         ok = false;
+      int gi = 0;
+      if (ok && J.gcf_index) {
+        gi = __ldg(J.gcf_index + (g - J.vis_base));
+        if ((unsigned)gi >= (unsigned)J.n_gcf) ok = false;
+      }
       bad = !ok;
       if (ok) {
         pk = make_int2(mx * J.G + sx, my * J.G + sy);
@@ -106,7 +111,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(BinBuffers b) {
         if (mx + h >= 0 && mx - h + 1 < J.N && my + h >= 0 && my - h + 1 < J.N) {
           int cx = min(max(mx, 0), J.N - 1) >> J.log2T;
           int cy = min(max(my, 0), J.N - 1) >> J.log2T;
-          key = J.tile_base + cy * J.ntx + cx;
+          key = J.tile_base + (cy * J.ntx + cx) * J.n_gcf + gi;
         }
       }
       b.packed[g] = pk;

@@ -19,11 +19,13 @@ int set_error(int code, const char *msg);
 struct BinJob {
   const void *uv;
   const void *vals;
+  const int *gcf_index;  // per-visibility table index, or null
   int64_t vis_base;
   int64_t npts;
-  int tile_base, ntiles;
+  int tile_base, ntiles;  // ntiles = ntx * ntx * n_gcf bins
   int N, S, G, log2G, log2T, ntx, P;
   int uv_f64;
+  int n_gcf;
 };
 
 struct BinBuffers {
@@ -102,9 +104,10 @@ struct GridLaunch {
 
 cudaError_t launch_scatter(const GridLaunch &g, cudaStream_t s);
 cudaError_t launch_window(const GridLaunch &g, cudaStream_t s);
-// Row-doubled copy of a [G*G][S][S] GCF table for the moving-window kernel:
-// dst[s][b][a] = src[s][b mod S][a] for b < 2S (elem_bytes 8 or 16)
-cudaError_t launch_gcf_double_rows(const void *src, void *dst, int S, int G,
+// Row-doubled copy of ntab consecutive [G*G][S][S] GCF tables for the
+// moving-window kernel: dst[s][b][a] = src[s][b mod S][a] for b < 2S, s over
+// all ntab*G*G sub-kernels (elem_bytes 8 or 16)
+cudaError_t launch_gcf_double_rows(const void *src, void *dst, int S, int G, int ntab,
                                    int elem_bytes, cudaStream_t s);
 inline size_t gcf_double_rows_bytes(int S, int G, int elem_bytes) {
   return (size_t)elem_bytes * G * G * 2 * S * S;

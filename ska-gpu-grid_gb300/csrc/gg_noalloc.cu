@@ -126,6 +126,8 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
     return noalloc_fail(GG_ERR_ARG,
                         "noalloc: img_dim exceeds the fixed scratch (max 16384 uv tiles, "
                         "i.e. 4096 at tile 32)");
+  if (job->gcf_index)
+    return noalloc_fail(GG_ERR_ARG, "noalloc: per-visibility GCF tables are not supported");
   if (opt->gcf_kind == GG_GCF_TABLE && (int64_t)G * G * S * S > kNoAllocMaxGcf)
     return noalloc_fail(GG_ERR_ARG,
                         "noalloc: GCF table exceeds the fixed scratch (G*G*S*S at most 65536, "
@@ -169,6 +171,7 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   const double sg = job->gcf_sigma > 0 ? job->gcf_sigma
                                        : (opt->gcf_sigma > 0 ? opt->gcf_sigma : S / 4.0);
   D.sigma = (float)sg;
+  D.n_gcf = 1;
   BinJob B;
   std::memset(&B, 0, sizeof B);
   B.uv = job->uv;
@@ -177,6 +180,7 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   B.npts = n;
   B.tile_base = 0;
   B.ntiles = (int)(ntx * ntx);
+  B.n_gcf = 1;
   B.N = (int)N;
   B.S = (int)S;
   B.G = G;
@@ -206,7 +210,7 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   GG_NA(cudaMemsetAsync(job->out, 0, out_bytes, s));
 
   if (opt->gcf_kind == GG_GCF_TABLE)
-    GG_NA(launch_gcf_double_rows(job->gcf, ws + kOffGcf, (int)S, G, 8, s));
+    GG_NA(launch_gcf_double_rows(job->gcf, ws + kOffGcf, (int)S, G, 1, 8, s));
 
   BinBuffers b{};
   b.jobs = (const BinJob *)(ws + kOffBin);

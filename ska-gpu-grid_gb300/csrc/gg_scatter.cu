@@ -81,8 +81,17 @@ __global__ void __launch_bounds__(kScatterThreads)
         } else if (!ok) {
           atomicAdd(&kp.flags[FLAG_INDEX], 1);
         }
+        int tab = 0;
+        if (ok && J.gcf_index) {
+          tab = __ldg(J.gcf_index + n);
+          if ((unsigned)tab >= (unsigned)J.n_gcf) {
+            ok = false;
+            atomicAdd(&kp.flags[FLAG_INDEX], 1);
+          }
+        }
         if (ok && mx + H >= 0 && mx - H + 1 < J.N && my + H >= 0 && my - H + 1 < J.N) {
-          r = make_int4(mx, my, sx | (sy << 8), j);
+          // sx, sy < 64 (8 bits each), table index < 32768
+          r = make_int4(mx, my, sx | (sy << 8) | (tab << 16), j);
           const VT2 *v = reinterpret_cast<const VT2 *>(J.vals) + n * P;
           for (int p = 0; p < P; ++p) sval[tid * P + p] = __ldg(v + p);
         }
@@ -96,12 +105,12 @@ __global__ void __launch_bounds__(kScatterThreads)
       const JobDesc &J = kp.jobs[r.w];
       const int N = J.N;
       const size_t NN = (size_t)N * N;
-      const int sx = r.z & 0xff, sy = r.z >> 8;
+      const int sx = r.z & 0xff, sy = (r.z >> 8) & 0xff, tab = r.z >> 16;
       GcfSrc<S, GAUSS, VT> gsrc;
       if constexpr (GAUSS) {
         gsrc.g1 = g1;
       } else {
-        gsrc.tab = reinterpret_cast<const VT2 *>(J.gcf);
+        gsrc.tab = reinterpret_cast<const VT2 *>(J.gcf) + (size_t)tab * J.G * J.G * S * S;
         gsrc.G = J.G;
       }
       for (int tap = lane; tap < S * S; tap += 32) {

@@ -30,6 +30,10 @@ struct JobDesc {
   int N, S, G, log2G, P, T, log2T, ntx;
   int planar, out_f64, uv_f64;
   float sigma;
+  // per-visibility GCF tables (1 = a single table); binned methods: the
+  // binning key of a visibility is tile * n_gcf + its table index
+  const int *gcf_index;  // scatter: the caller's per-visibility indices
+  int n_gcf;
 };
 
 // A slice of one uv tile's sorted visibilities: the unit of the device work

@@ -289,7 +289,10 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
     const WorkItem w = kp.items[item];
     const JobDesc &J = kp.jobs[w.job];
     const int N = J.N, log2G = J.log2G;
-    const int tx = w.bin % J.ntx, ty = w.bin / J.ntx;
+    // bin = uv tile * n_gcf + table index (per-visibility GCF tables)
+    const int tile = J.n_gcf > 1 ? w.bin / J.n_gcf : w.bin;
+    const int tab = w.bin - tile * J.n_gcf;
+    const int tx = tile % J.ntx, ty = tile / J.ntx;
     const int ox = tx * T - H + 1, oy = ty * T - H + 1;  // sub-grid origin
     const int n = w.end - w.start;
     const int nch = (n + K - 1) / K;
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
     };
     if (leader) issue_next(gfirst + 2);
 
-    const VT2 *gtab = reinterpret_cast<const VT2 *>(J.gcf);
+    const VT2 *gtab = reinterpret_cast<const VT2 *>(J.gcf) + (size_t)tab * J.G * J.G * 2 * S * S;
     const int G = J.G;
     // tiles on the border of the grid hold the clamped mains, whose
     // footprints may leave the sub-grid
@@ -647,12 +650,12 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-cudaError_t launch_gcf_double_rows(const void *src, void *dst, int S, int G, int elem_bytes,
-                                   cudaStream_t s) {
-  const int64_t n = 2ll * G * G * S * S;
+cudaError_t launch_gcf_double_rows(const void *src, void *dst, int S, int G, int ntab,
+                                   int elem_bytes, cudaStream_t s) {
+  const int64_t n = 2ll * ntab * G * G * S * S;
   const int blocks = (int)std::min<int64_t>((n + 255) / 256, 1184);
   gcf_double_rows_kernel<<<blocks, 256, 0, s>>>((const unsigned char *)src, (unsigned char *)dst,
-                                                 S, G * G, elem_bytes);
+                                                 S, ntab * G * G, elem_bytes);
   count_launch();
   return cudaGetLastError();
 }

@@ -66,7 +66,8 @@ class gg_job(ctypes.Structure):
                 ("gcf_dim", ctypes.c_int64), ("uv_type", ctypes.c_int32),
                 ("vals_type", ctypes.c_int32), ("out_type", ctypes.c_int32),
                 ("reserved0", ctypes.c_int32), ("gcf_sigma", ctypes.c_double),
-                ("reserved", ctypes.c_int64 * 4)]
+                ("gcf_index", ctypes.c_void_p), ("n_gcf", ctypes.c_int64),
+                ("reserved", ctypes.c_int64 * 2)]
 
 
 REQ_INPUTS_ON_DEVICE, REQ_OUT_ON_DEVICE, REQ_KEEP_RESIDENT = 1, 2, 4
@@ -318,7 +319,10 @@ class Context:
 
     @staticmethod
     def make_job(out, uv, vals, gcf, img_dim: int, gcf_dim: int,
-                 npts: int | None = None, gcf_sigma: float = 0.0) -> gg_job:
+                 npts: int | None = None, gcf_sigma: float = 0.0,
+                 gcf_index=None, n_gcf: int = 1) -> gg_job:
+        """gg_job over device tensors.  gcf_index (int32, one per visibility)
+        selects one of n_gcf consecutive [G*G][S][S] tables at gcf."""
         j = gg_job()
         j.out = out.data_ptr()
         j.uv = uv.data_ptr() if uv is not None else None
@@ -330,6 +334,9 @@ class Context:
         j.vals_type = _ttype(vals) if vals is not None else C64
         j.out_type = _ttype(out)
         j.gcf_sigma = gcf_sigma
+        if gcf_index is not None:
+            j.gcf_index = gcf_index.data_ptr()
+            j.n_gcf = int(n_gcf)
         return j
 
     def grid_job(self, opts: Options, job: gg_job, stream=None) -> None:

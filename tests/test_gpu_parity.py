@@ -332,6 +332,58 @@ def test_batch_of_track_jobs_matches_oracle(ctx, accum, autotune):
             assert "support 8 " in report and "support 16 " in report
 
 
+@pytest.mark.parametrize("mode,prec", [("scatter", "cc_comp"), ("window", "cc_comp"),
+                                       ("window", "cc"), ("window", "zz")])
+def test_per_visibility_gcf_tables(ctx, mode, prec):
+    """A table per visibility (w-plane / baseline GCFs, the reference's
+    vis.gcfinx): two jobs in one batch with 3 and 5 tables (one complex),
+    dense tracks, indices outside the stack dropped and counted; against the
+    oracle's per-visibility restatement."""
+    vdt = np.complex128 if prec == "zz" else np.complex64
+    o = opts_for(mode, prec, layout=gg.LAYOUT_INTERLEAVED)
+    keep, jobs, refs, dropped = [], [], [], 0
+    for k, (N, S, ntab) in enumerate([(256, 8, 3), (512, 16, 5)]):
+        uv, vals = synth.tracks(N, nant=16, ntime=800, npts=None, seed=400 + k,
+                                vals_dtype=vdt)
+        rng = np.random.default_rng(500 + k)
+        idx = rng.integers(0, ntab, len(uv)).astype(np.int32)
+        idx[::211] = ntab          # outside the stack
+        dropped += int((idx == ntab).sum())
+        tabs = [synth.gcf_table(synth.gaussian_gcf_1d(S, sigma=S / 4 + 0.3 * t)).astype(vdt)
+                for t in range(ntab)]
+        tabs[1] = (tabs[1] * np.exp(0.9j)).astype(vdt)
+        stack = np.concatenate([t.reshape(-1) for t in tabs])
+        odt = torch.complex128 if prec == "zz" else torch.complex64
+        d = [torch.from_numpy(uv).cuda(), torch.from_numpy(vals).cuda(),
+             torch.from_numpy(stack).cuda(),
+             torch.full((N * N,), float("nan"), dtype=odt, device="cuda"),
+             torch.from_numpy(idx).cuda()]
+        keep.append(d)
+        jobs.append(gg.Context.make_job(d[3], d[0], d[1], d[2], N, S, gcf_index=d[4],
+                                        n_gcf=ntab))
+        refs.append((N, O.grid_pz_gcfinx(uv, vals, idx, stack, N, S, nthreads=8)))
+    ctx.grid_batch(o, jobs)
+    torch.cuda.synchronize()
+    flags = ctx.read_flags()
+    assert flags[0] == dropped and flags[1:] == [0, 0, 0]
+    for (N, ref), d in zip(refs, keep):
+        host = torch.view_as_real(d[3]).reshape(-1).cpu().numpy()
+        assert rel_err(planar_from_grid(host, 1, N, False), ref) <= TOL[prec]
+
+
+def test_per_visibility_gcf_rejected_by_gather(ctx):
+    N, S = 64, 8
+    d = [torch.zeros((10, 2), dtype=torch.float64, device="cuda"),
+         torch.zeros(10, dtype=torch.complex64, device="cuda"),
+         torch.zeros(64 * S * S * 2, dtype=torch.complex64, device="cuda"),
+         torch.zeros(N * N, dtype=torch.complex64, device="cuda"),
+         torch.zeros(10, dtype=torch.int32, device="cuda")]
+    j = gg.Context.make_job(d[3], d[0], d[1], d[2], N, S, gcf_index=d[4], n_gcf=2)
+    with pytest.raises(gg.GridError) as e:
+        ctx.grid_batch(opts_for("gather", "cc_comp"), [j])
+    assert e.value.code == gg.ERR_ARG and "gcf_index" in str(e.value)
+
+
 # ---------------------------------------------------------------------------
 # drop-in host entry points (padded buffers, reference semantics)
 # ---------------------------------------------------------------------------

@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+import synth
 from helpers import GOLDEN_CASES, load_golden
 
 REF_TAGS = ["64_8_1_double", "64_8_4_double", "64_32_1_double",
@@ -117,3 +118,22 @@ def test_gaussian_gcf_is_separable_and_peaks_at_centre():
     assert g1[0].argmax() == 16 // 2 - 1 and g1[0].max() == 1.0
     t2 = O.gcf_from_1d(g1)
     assert np.array_equal(tab, t2)
+
+
+def test_oracle_per_visibility_tables():
+    """gridCPU_pz with a table per visibility (vis.gcfinx): one table is the
+    plain oracle bit for bit; several tables = the sum of per-table grids;
+    indices outside the stack are skipped."""
+    uv, v = synth.uniform(4000, 4, 60, seed=11)
+    S = 8
+    tabs = [synth.gcf_table(synth.gaussian_gcf_1d(S, sigma=sg)) for sg in (1.5, 2.0, 2.5)]
+    tabs[1] = tabs[1] * np.exp(0.7j)  # a complex table
+    stack = np.concatenate([t.reshape(-1) for t in tabs])
+    one = O.grid_pz_gcfinx(uv, v, np.zeros(len(uv), np.int32), tabs[0].reshape(-1), 64, S)
+    assert np.array_equal(one, O.grid_pz(uv, v, tabs[0], 64, S))
+    idx = (np.arange(len(uv)) * 7 % 3).astype(np.int32)
+    idx[::97] = 5
+    idx[1::101] = -1
+    got = O.grid_pz_gcfinx(uv, v, idx, stack, 64, S, nthreads=4)
+    want = sum(O.grid_pz(uv[idx == k], v[idx == k], tabs[k], 64, S) for k in range(3))
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
