@@ -105,6 +105,24 @@ def pairs(c):
     return np.stack([c.real, c.imag], -1).astype(np.float64)
 
 
+def max_over_ranks(x, dist, dev=None):
+    """the largest value of x over all ranks (x unchanged without a process
+    group): every rank's timed region ends when the slowest rank's does"""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64,
+                     device=dev if dev is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank, world, seconds):
+    """whole-job throughput of `world` replicas that each processed
+    units_per_rank in `seconds` (the max over ranks), in millions per second"""
+    return world * units_per_rank / seconds / 1e6
+
+
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
@@ -364,11 +382,8 @@ def run_served(args, rank, world, local_rank, dist):
         torch.cuda.synchronize()
     launches = gg.kernel_launches() - l0
     total_s = sum(spans)
-    if dist:
-        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * total_vis * args.steps / total_s / 1e6
+    total_s = max_over_ranks(total_s, dist, dev)
+    value = replica_rate(total_vis * args.steps, world, total_s)
 
     # arrival-rate sweep (Poisson) up to saturation
     rng = np.random.default_rng(11)
@@ -507,7 +522,8 @@ def run_served(args, rank, world, local_rank, dist):
                 srv.release(tt)
             t_all += time.perf_counter() - t0
         reps = max(1, min(args.steps, 3))
-        e2e = {"value": round(world * total_vis * reps / t_all / 1e6, 3), "unit": "Mvis/s",
+        t_all = max_over_ranks(t_all, dist, dev)
+        e2e = {"value": round(replica_rate(total_vis * reps, world, t_all), 3), "unit": "Mvis/s",
                "h2d_bytes_per_step": int(total_vis * 24),
                "d2h_bytes_per_step": int(sum(8 * int(N) * int(N) for N in specs["side"])),
                "ms_per_step": round(1e3 * t_all / reps, 3),
@@ -615,11 +631,8 @@ def run_batch(args, rank, world, local_rank, dist):
     # graph replays launch the captured kernels without the library's counter
     launches = (gg.kernel_launches() - l0) or None
     total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    if dist:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * total_vis * args.steps / (total_ms / 1e3) / 1e6
+    total_ms = max_over_ranks(total_ms, dist, dev)
+    value = replica_rate(total_vis * args.steps, world, total_ms / 1e3)
     # number of kernels in one replay: count a direct (uncaptured) launch
     l1 = gg.kernel_launches()
     plan.launch()
@@ -688,7 +701,8 @@ def run_batch(args, rank, world, local_rank, dist):
                 srv.release(int(t))
         t_all = time.perf_counter() - t0
         srv.close()
-        e2e = {"value": round(world * total_vis * reps / t_all / 1e6, 3), "unit": "Mvis/s",
+        t_all = max_over_ranks(t_all, dist, dev)
+        e2e = {"value": round(replica_rate(total_vis * reps, world, t_all), 3), "unit": "Mvis/s",
                "h2d_bytes_per_step": int(total_vis * 24),
                "d2h_bytes_per_step": int(sum(8 * int(N) * int(N) for N in specs["side"])),
                "ms_per_step": round(1e3 * t_all / reps, 3),
@@ -830,10 +844,7 @@ def run_single(args, rank, world, local_rank, dist):
         torch.cuda.synchronize()
     launches = gg.kernel_launches() - l0
     total_ms = sum(s.elapsed_time(e) for s, e in zip(start, end))
-    if dist:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist, dev)
     e2e = None
     if not args.no_e2e:
         pin_uv = torch.from_numpy(uv.view(np.complex128).reshape(-1)).pin_memory().numpy()
@@ -850,18 +861,15 @@ def run_single(args, rank, world, local_rank, dist):
             gg.grid_host(o, pin_out, pin_uv, pin_vals, n, N, pin_gcf, S)
             ts.append(time.perf_counter() - t0)
         e2e_s = sum(ts)
-        if dist:
-            t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": round(world * n * args.steps / e2e_s / 1e6, 3), "unit": "Mvis/s",
+        e2e_s = max_over_ranks(e2e_s, dist, dev)
+        e2e = {"value": round(replica_rate(n * args.steps, world, e2e_s), 3), "unit": "Mvis/s",
                "h2d_bytes_per_step": int(pin_uv.nbytes + pin_vals.nbytes + pin_gcf.nbytes),
                "d2h_bytes_per_step": int(N * N * pin_out.itemsize),
                "ms_per_step": round(1e3 * e2e_s / args.steps, 4),
                "api": "gg_grid_host (C ABI, pinned host buffers)"}
     if rank != 0:
         return None
-    value = world * n * args.steps / (total_ms / 1e3) / 1e6
+    value = replica_rate(n * args.steps, world, total_ms / 1e3)
     vb = 8 if w["vals"] == "c64" else 16
     ob = 8 if w["out"] == "c64" else 16
     mode_name = {0: "scatter", 1: "gather", 2: "window", 3: "window"}[o.mode]
