@@ -751,6 +751,7 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
     b.flags = flags;
     b.input_sorted = pl.input_sorted;
     b.kept_pos = pl.input_sorted ? (int *)(ws + pl.o_kept) : nullptr;
+    b.window_records = pl.mode == GG_MODE_WINDOW;
     GG_CUDA(run_binning(b, s));
   }
 

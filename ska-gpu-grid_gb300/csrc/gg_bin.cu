@@ -159,9 +159,13 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(BinBuffers b) {
       if (key >= 0) pos = start + __popc(peers & lanemask_lt());
     }
     if (pos >= 0) {
-      b.sorted_idx[pos] = b.packed[g];
       int j = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, g);
       const BinJob &J = b.jobs[j];
+      const int2 pk = b.packed[g];
+      b.sorted_idx[pos] = b.window_records
+                              ? window_record(pk.x >> J.log2G, pk.x & (J.G - 1),
+                                              pk.y >> J.log2G, pk.y & (J.G - 1), J.G)
+                              : pk;
       int64_t n = g - J.vis_base;
       if (b.vals_bytes == 8) {
         const float2 *v = (const float2 *)J.vals + n * b.P;

@@ -49,7 +49,20 @@ struct BinBuffers {
   int *flags;
   int input_sorted;
   int *kept_pos;           // [total_vis+1] (input_sorted only)
+  // sorted record format: 0 = packed (main*G+sub) pairs (gather, gg_bin);
+  // 1 = moving window: {main cells (my+64)<<16 | (mx+64), sub-kernel
+  //     sy*G+sx} -- see window_record()
+  int window_records;
 };
+
+// Sorted record of the moving-window kernel: both main cells in one word
+// (offset by 64 so that clamped mains stay positive; 16 bits each hold
+// img_dim up to 32768 plus the support) and the sub-kernel index.
+constexpr int kWinMainBias = 64;
+__host__ __device__ inline int2 window_record(int mx, int sx, int my, int sy, int G) {
+  return make_int2((int)(((unsigned)(my + kWinMainBias) << 16) | (unsigned)(mx + kWinMainBias)),
+                   sy * G + sx);
+}
 
 // index step only (vis2ints)
 cudaError_t launch_vis2ints(int uv_f64, const void *uv, int64_t npts, int G,

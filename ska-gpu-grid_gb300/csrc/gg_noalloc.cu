@@ -232,6 +232,7 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   b.order = nullptr;
   b.flags = flags;
   b.input_sorted = opt->input_sorted ? 1 : 0;
+  b.window_records = 1;
   b.kept_pos = b.input_sorted ? (int *)(ws + kOffKept) : nullptr;
   GG_NA(run_binning(b, s));
 

@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
     int cur[Q];
     // footprint origin of the last record, this thread's column in it and
     // the offset of its first tap in a sub-kernel of the row-doubled table
-    int pfx = INT_MIN, pfy = INT_MIN, pax = 0, pofs = 0, pkx = 0, pky = 0;
+    int pfx = INT_MIN, pfy = INT_MIN, pax = 0, pofs = 0, pkm = -1;
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
       acc[k].zero();
@@ -366,8 +366,9 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
       // ([G*G][2S][S]): this thread's Q taps of a record, rows b0 + k*D mod S,
       // then sit at fixed strides k*D*S from its first tap.
       constexpr int D = NGT / S;
-      auto load_g = [&](GT (&g)[Q], int sx, int sy) {
+      auto load_g = [&](GT (&g)[Q], int sub) {
         if constexpr (GAUSS) {
+          const int sx = sub & (G - 1), sy = sub >> log2G;
           const float gxf = g1[sx * 2 * S + pax];
           const float *gy = g1 + sy * 2 * S + pofs;
 #pragma unroll
@@ -376,7 +377,7 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
             g[k].y = 0;
           }
         } else {
-          const GT *gp = reinterpret_cast<const GT *>(gtab) + (sy * G + sx) * (2 * S * S) + pofs;
+          const GT *gp = reinterpret_cast<const GT *>(gtab) + sub * (2 * S * S) + pofs;
 #pragma unroll
           for (int k = 0; k < Q; ++k) g[k] = __ldg(gp + k * D * S);
         }
@@ -413,8 +414,8 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
         const int r2 = min(r + 2, m - 1);
         const int2 q = ib[r2];
         vc = vb[r2];
-        nc = (((q.x ^ pkx) | (q.y ^ pky)) & ~(G - 1)) == 0 && r + 2 < mr;
-        load_g(gc, unpack_sub(q.x, log2G), unpack_sub(q.y, log2G));
+        nc = q.x == pkm && r + 2 < mr;
+        load_g(gc, q.y);
         accum(ga, va);
       };
       auto run_interior = [&]() {
@@ -423,8 +424,8 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
           // slow step: record r opens a run
           const int2 pk = ib[r];
           VT2 va = vb[r], vb1, vc1;
-          const int fx0 = unpack_main(pk.x, log2G) - H + 1;
-          const int fy0 = unpack_main(pk.y, log2G) - H + 1;
+          const int fx0 = (int)((unsigned)pk.x & 0xffffu) - kWinMainBias - H + 1;
+          const int fy0 = (int)((unsigned)pk.x >> 16) - kWinMainBias - H + 1;
           if (MODE == 1 && run >= kRunMax) flush_runs();
           if (fx0 != pfx || fy0 != pfy) {
             pfx = fx0;
@@ -444,19 +445,17 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
               }
             }
           }
-          // the packed main cells of this run (the oversample bits masked
-          // out when comparing) and the last record the run may reach
-          pkx = pk.x;
-          pky = pk.y;
+          // the main cells of this run and the last record the run may reach
+          pkm = pk.x;
           const int r0 = r;
           const int mr = MODE == 1 ? min(m, r0 + (kRunMax - run)) : m;
           GT ga[Q], gb[Q], gc[Q];
-          load_g(ga, unpack_sub(pk.x, log2G), unpack_sub(pk.y, log2G));
+          load_g(ga, pk.y);
           const int r1 = min(r + 1, m - 1);
           const int2 q = ib[r1];
           vb1 = vb[r1];
-          bool nb = (((q.x ^ pkx) | (q.y ^ pky)) & ~(G - 1)) == 0 && r + 1 < mr, nc, na;
-          load_g(gb, unpack_sub(q.x, log2G), unpack_sub(q.y, log2G));
+          bool nb = q.x == pkm && r + 1 < mr, nc, na;
+          load_g(gb, q.y);
           // fast loop over the rest of the run, three rotating stages
           for (;;) {
             step(r++, mr, ga, va, gc, vc1, nc);
@@ -479,8 +478,9 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
           if (MODE == 1 && ++run >= kRunMax) flush_runs();
           const int2 pk = ib[r];
           const VT2 v = vb[r];
-          const int mx = unpack_main(pk.x, log2G), sx = unpack_sub(pk.x, log2G);
-          const int my = unpack_main(pk.y, log2G), sy = unpack_sub(pk.y, log2G);
+          const int mx = (int)((unsigned)pk.x & 0xffffu) - kWinMainBias;
+          const int my = (int)((unsigned)pk.x >> 16) - kWinMainBias;
+          const int sx = pk.y & (G - 1), sy = pk.y >> log2G;
           const int fx0 = mx - H + 1, fy0 = my - H + 1;
           const int ap = (rx - fx0) & (S - 1);
           const int lx = fx0 + ap - bx;
