@@ -111,6 +111,7 @@ int gg_autotune_report(char *buf, size_t len);
 const char *gg_last_error(void);
 int gg_abi_version(void);
 
+
 /* ---- drop-in gridGPU: HOST buffers, reference semantics ----------------
  * out: (img_dim^2 + 2*img_dim*gcf_dim + 2*gcf_dim) * P elements; the grid is
  * written at element offset img_dim*gcf_dim + gcf_dim and everything else is
@@ -139,6 +140,20 @@ typedef struct gg_context gg_context;
 
 int gg_create(gg_context **ctx, int device);
 int gg_destroy(gg_context *ctx);
+
+/* ---- failure detection, tested without a GPU fault ---------------------
+ * Every device-side wait of the library (mbarrier phases of the bulk copies)
+ * gives up after a bounded time (0.5 s), raises the context's timeout flag
+ * (gg_read_flags()[1]) and lets the kernel return.
+ * gg_selftest_wait_timeout runs one warp that waits on an mbarrier nothing
+ * completes; it returns GG_ERR_TIMEOUT when the wait gave up as designed
+ * (the context stays usable) and GG_ERR_STATE otherwise.
+ * gg_debug_inject_alloc_failures makes the next `count` device allocations
+ * of the library fail with GG_ERR_NOMEM (0 switches it off): a test hook for
+ * allocation-failure paths. */
+int gg_selftest_wait_timeout(gg_context *ctx, void *stream);
+int gg_debug_inject_alloc_failures(int32_t count);
+
 /* Pre-size the context's device workspace for jobs up to these sizes so that
  * later calls allocate nothing (needed before CUDA-graph capture). */
 int gg_reserve(gg_context *ctx, const gg_options *opt, int64_t max_npts,

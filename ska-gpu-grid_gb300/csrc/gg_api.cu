@@ -67,6 +67,14 @@ static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 // ---------------------------------------------------------------------------
 // device buffer that only grows
 // ---------------------------------------------------------------------------
+static std::atomic<int> g_fail_allocs{0};
+bool injected_alloc_failure() {
+  int k = g_fail_allocs.load();
+  while (k > 0)
+    if (g_fail_allocs.compare_exchange_weak(k, k - 1)) return true;
+  return false;
+}
+
 struct DevBuf {
   void *p = nullptr;
   size_t n = 0;
@@ -75,6 +83,8 @@ struct DevBuf {
     if (p) cudaFree(p);
     p = nullptr;
     n = 0;
+    if (injected_alloc_failure())
+      return fail(GG_ERR_NOMEM, "cudaMalloc(workspace): injected allocation failure");
     size_t want = align256(bytes + bytes / 8);
     cudaError_t e = cudaMalloc(&p, want);
     if (e != cudaSuccess) {
@@ -974,6 +984,29 @@ int gg_get_global_options(gg_options *opt) {
   std::lock_guard<std::mutex> lk(g_opt_mu);
   *opt = g_global_opts;
   return GG_OK;
+}
+
+int gg_debug_inject_alloc_failures(int32_t count) {
+  if (count < 0) return fail(GG_ERR_ARG, "count < 0");
+  g_fail_allocs.store(count);
+  return GG_OK;
+}
+
+int gg_selftest_wait_timeout(gg_context *ctx, void *stream) {
+  if (!ctx) return fail(GG_ERR_ARG, "ctx: null");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  GG_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  int *flags = (int *)ctx->flags.p;
+  GG_CUDA(cudaMemsetAsync(flags + FLAG_TIMEOUT, 0, sizeof(int), s));
+  GG_CUDA(launch_selftest_wait(flags, s));
+  int h = 0;
+  GG_CUDA(cudaMemcpyAsync(&h, flags + FLAG_TIMEOUT, sizeof h, cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  GG_CUDA(cudaMemsetAsync(flags + FLAG_TIMEOUT, 0, sizeof(int), s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  if (h) return fail(GG_ERR_TIMEOUT, "device wait gave up after its limit (expected)");
+  return fail(GG_ERR_STATE, "device wait did not report a timeout");
 }
 
 int gg_autotune_clear(void) {

@@ -273,16 +273,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: every waiter gives up after kSpinLimit polls (each try_wait
-// itself suspends for a hardware-defined interval), raises the context's
+// Bounded wait: every waiter gives up once kWaitLimitNs of wall-clock time
+// (the global timer) have passed without the phase completing -- or after
+// kSpinLimit polls, should the timer not advance -- raises the context's
 // timeout flag and reports failure, so a lost completion can never hang the
-// GPU.  A bulk copy of valid global memory always completes; the limit only
-// guards against a bug.
-constexpr uint32_t kSpinLimit = 1u << 22;
+// GPU.  A bulk copy of valid global memory completes in microseconds; the
+// limit only guards against a bug.
+constexpr uint64_t kWaitLimitNs = 500000000ull;  // 0.5 s
+constexpr uint32_t kSpinLimit = 1u << 26;
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
                                           int *flags) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t i = 1; i < kSpinLimit; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63) == 0 && global_ns() - t0 > kWaitLimitNs) break;
+  }
   if (flags) atomicOr(&flags[FLAG_TIMEOUT], 1);
   return false;
 }

@@ -117,6 +117,11 @@ struct GridLaunch {
 
 cudaError_t launch_scatter(const GridLaunch &g, cudaStream_t s);
 cudaError_t launch_window(const GridLaunch &g, cudaStream_t s);
+// one warp waiting on an mbarrier nobody completes (bounded-wait self-test)
+cudaError_t launch_selftest_wait(int *flags, cudaStream_t s);
+// test hook: the next n device allocations of the library fail (NOMEM);
+// returns true (and consumes one) when the current allocation must fail
+bool injected_alloc_failure();
 // Row-doubled copy of ntab consecutive [G*G][S][S] GCF tables for the
 // moving-window kernel: dst[s][b][a] = src[s][b mod S][a] for b < 2S, s over
 // all ntab*G*G sub-kernels (elem_bytes 8 or 16)

@@ -183,7 +183,8 @@ void launch_batch(gg_server *srv, Slot *slot) {
     } else if (r.npts > 0) {
       const size_t bu = (size_t)r.npts * elem(r.uv_type);
       const size_t bv = (size_t)r.npts * elem(r.vals_type) * P;
-      e = cudaMallocAsync(&q->d_uv, bu, s);
+      e = gg::injected_alloc_failure() ? cudaErrorMemoryAllocation
+                                       : cudaMallocAsync(&q->d_uv, bu, s);
       if (e == cudaSuccess) {
         q->own_uv = true;
         e = cudaMallocAsync(&q->d_vals, bv, s);
@@ -198,7 +199,10 @@ void launch_batch(gg_server *srv, Slot *slot) {
       if (r.flags & GG_REQ_OUT_ON_DEVICE) {
         q->d_out = r.out;
       } else {
-        e = cudaMallocAsync(&q->d_out, (size_t)elem(r.out_type) * P * r.img_dim * r.img_dim, s);
+        e = gg::injected_alloc_failure()
+                ? cudaErrorMemoryAllocation
+                : cudaMallocAsync(&q->d_out, (size_t)elem(r.out_type) * P * r.img_dim * r.img_dim,
+                                  s);
         if (e == cudaSuccess) q->own_out = true;
       }
     }

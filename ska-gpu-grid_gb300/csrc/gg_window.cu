@@ -660,6 +660,26 @@ cudaError_t launch_gcf_double_rows(const void *src, void *dst, int S, int G, int
   return cudaGetLastError();
 }
 
+// Self-test of the bounded wait: an mbarrier that expects one arrival which
+// never comes.  Every thread waits on it with mbar_wait, gives up after the
+// wait limit and raises the timeout flag; no copy is in flight, so nothing is
+// left behind.
+__global__ void __launch_bounds__(32) selftest_wait_kernel(int *flags) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  mbar_wait(&bar, 0, flags);
+}
+
+cudaError_t launch_selftest_wait(int *flags, cudaStream_t s) {
+  selftest_wait_kernel<<<1, 32, 0, s>>>(flags);
+  count_launch();
+  return cudaGetLastError();
+}
+
 cudaError_t launch_window(const GridLaunch &g, cudaStream_t s) {
   KParams kp{};
   kp.jobs = g.jobs;

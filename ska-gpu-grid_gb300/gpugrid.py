@@ -155,6 +155,8 @@ def _load():
         "gg_server_drain": ([vp, ctypes.c_double], ctypes.c_int),
         "gg_server_destroy": ([vp], ctypes.c_int),
         "gg_autotune_clear": ([], ctypes.c_int),
+        "gg_selftest_wait_timeout": ([vp, vp], ctypes.c_int),
+        "gg_debug_inject_alloc_failures": ([i32], ctypes.c_int),
         "gg_autotune_report": ([ctypes.c_char_p, sz], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
