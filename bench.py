@@ -780,6 +780,8 @@ def run_single(args, rank, world, local_rank, dist):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     w = WORKLOADS[args.workload]
+    if args.method:
+        w = dict(w, mode=args.method)
     N, S, n = w["N"], w["S"], w["npts"]
     uv, vals, gcf = make_single(w, seed=1000 + rank)
     o = single_options(w)
@@ -989,6 +991,9 @@ def main():
                     help="seconds of CPU gridding for the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--method", choices=["scatter", "gather", "window"], default=None,
+                    help="single-job workloads: grid with this method instead of the "
+                         "workload's own")
     args = ap.parse_args()
     if args.warmup < 3:
         log("bench: warm-up below 3 steps; using 3")

@@ -50,7 +50,8 @@ extern "C" {
 #define GG_MODE_SCATTER 0 /* per-tap native red.global adds                  */
 #define GG_MODE_GATHER 1  /* one output cell per thread over uv-tile bins    */
 #define GG_MODE_WINDOW 2  /* register + shared-memory moving window per tile */
-#define GG_MODE_AUTO 3    /* autotuner's choice for the size class           */
+#define GG_MODE_AUTO 3    /* moving window for FP32 values, scatter for FP64
+                             values (the faster on this GPU for each)        */
 
 /* ---- output layout ----------------------------------------------------- */
 #define GG_LAYOUT_INTERLEAVED 0 /* P planes of N*N (re,im) pairs             */

@@ -278,10 +278,15 @@ static void ctx_release(gg_context *c) {
   if (c->own) cudaStreamDestroy(c->own);
 }
 
-static int resolve_mode(const gg_options *o, int S) {
+// GG_MODE_AUTO: the moving window for FP32 values (fastest at every size
+// class measured: 1.5x scatter on the 4096^2 track workload, more on
+// batches); the scatter for FP64 values, whose FP64 register arithmetic in
+// the window kernel is slower on this GPU than FP64 L2 reductions (1024^2,
+// S=16: 399 vs 218 Mvis/s)
+static int resolve_mode(const gg_options *o, int S, int vals_f64) {
   if (o->mode != GG_MODE_AUTO) return o->mode;
   (void)S;
-  return GG_MODE_WINDOW;  // measured fastest at every size class so far
+  return vals_f64 ? GG_MODE_SCATTER : GG_MODE_WINDOW;
 }
 
 // Launch configuration of one support class of the moving window
@@ -374,7 +379,7 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
   {
     int64_t maxS = 0;
     for (int j = 0; j < njobs; ++j) maxS = std::max<int64_t>(maxS, jobs[j].gcf_dim);
-    const int m0 = resolve_mode(opt, (int)maxS);
+    const int m0 = resolve_mode(opt, (int)maxS, jobs[0].vals_type == GG_C128);
     const int vf64 = jobs[0].vals_type == GG_C128;
     for (int j = 0; j < njobs; ++j) {
       const int S = (int)jobs[j].gcf_dim;
@@ -454,7 +459,7 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
       if (opt->input_sorted)
         return fail(GG_ERR_ARG, "job %d: gcf_index with input_sorted is not supported", j);
     }
-    const int m = resolve_mode(opt, (int)J.gcf_dim);
+    const int m = resolve_mode(opt, (int)J.gcf_dim, J.vals_type == GG_C128);
     if (mode < 0) mode = m;
     if (m != mode) return fail(GG_ERR_ARG, "job %d: mixed methods in one batch", j);
     double sg = J.gcf_sigma > 0 ? J.gcf_sigma
@@ -856,7 +861,7 @@ static int autotune_batch(gg_context *c, const gg_options *opt, const gg_job *jo
   if (!opt->autotune || !tunable(opt) || njobs < 1 || !jobs) return GG_OK;
   int maxS = 0;
   for (int j = 0; j < njobs; ++j) maxS = std::max<int>(maxS, (int)jobs[j].gcf_dim);
-  if (resolve_mode(opt, maxS) != GG_MODE_WINDOW) return GG_OK;
+  if (resolve_mode(opt, maxS, jobs[0].vals_type == GG_C128) != GG_MODE_WINDOW) return GG_OK;
   const int vf64 = jobs[0].vals_type == GG_C128;
   cudaEvent_t e0, e1;
   GG_CUDA(cudaEventCreate(&e0));
