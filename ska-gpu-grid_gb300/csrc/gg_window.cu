@@ -532,13 +532,24 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
       }
     if (!direct) {
       group_sync(gid, NGT);  // all register sums are in the sub-grid
+      // walk cell i = gt, gt + NGT, ... keeping its (x, y) by increments (R
+      // is not a power of two: no division per cell)
+      const int sdx = NGT % R, sdy = NGT / R;
+      int cx = gt % R, cy = gt / R;
       for (int i = gt; i < R * R; i += NGT) {
         const CellT cv = region[i];
-        if (!cell_nonzero(cv)) continue;
-        region[i] = CellT{};
-        const int gx = ox + i % R, gy = oy + i / R;
-        if ((unsigned)gx < (unsigned)N && (unsigned)gy < (unsigned)N)
-          out_cell(J, (size_t)gy * N + gx, p, P, cv);
+        if (cell_nonzero(cv)) {
+          region[i] = CellT{};
+          const int gx = ox + cx, gy = oy + cy;
+          if ((unsigned)gx < (unsigned)N && (unsigned)gy < (unsigned)N)
+            out_cell(J, (size_t)gy * N + gx, p, P, cv);
+        }
+        cx += sdx;
+        cy += sdy;
+        if (cx >= R) {
+          cx -= R;
+          ++cy;
+        }
       }
     }
     // advance the stream: next plane of this item, or the next item
