@@ -213,8 +213,11 @@ struct Plan {
     const void *src;
     size_t off;
     int S;
-    int ntab;  // consecutive tables (per-visibility selection)
+    int ntab;         // consecutive tables (per-visibility selection)
+    size_t off_real;  // real parts (complex64 tables; 0: none)
   };
+  size_t o_gcf_flags = 0;  // one int per copy: nonzero when a table has imaginary parts
+  std::vector<size_t> hgcf_copy;  // per job (class order): index of its copy
   std::vector<GcfCopy> gcf_copies;
   std::vector<size_t> hgcf_off;
   // workspace carve (offsets into the device workspace)
@@ -542,8 +545,9 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
   pl.o_lo = pl.comp_lo ? take(lo_total) : 0;
   pl.gcf_copies.clear();
   pl.hgcf_off.assign(njobs, SIZE_MAX);
+  pl.hgcf_copy.assign(njobs, SIZE_MAX);
   if (mode == GG_MODE_WINDOW && !pl.gauss) {
-    std::map<std::tuple<const void *, int, int>, size_t> seen;
+    std::map<std::tuple<const void *, int, int>, size_t> seen;  // -> copy index
     for (int k = 0; k < njobs; ++k) {
       const gg_job &J = jobs[order[k]];
       const int ntab = J.gcf_index ? (int)J.n_gcf : 1;
@@ -551,11 +555,16 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
       auto it = seen.find(key);
       if (it == seen.end()) {
         const size_t o = take(gcf_double_rows_bytes((int)J.gcf_dim, pl.G, (int)vbytes) * ntab);
-        it = seen.emplace(key, o).first;
-        pl.gcf_copies.push_back({std::get<0>(key), o, (int)J.gcf_dim, ntab});
+        // complex64 tables: also their real parts, for the real-factor path
+        const size_t o_real =
+            vbytes == 8 ? take(gcf_double_rows_bytes((int)J.gcf_dim, pl.G, 4) * ntab) : 0;
+        it = seen.emplace(key, pl.gcf_copies.size()).first;
+        pl.gcf_copies.push_back({std::get<0>(key), o, (int)J.gcf_dim, ntab, o_real});
       }
-      pl.hgcf_off[k] = it->second;
+      pl.hgcf_copy[k] = it->second;
+      pl.hgcf_off[k] = pl.gcf_copies[it->second].off;
     }
+    pl.o_gcf_flags = take(sizeof(int) * (pl.gcf_copies.size() + 1));
   }
   pl.ws_bytes = off;
 
@@ -668,7 +677,12 @@ static void plan_bind(const gg_options *opt, Plan &pl, char *ws, char *host) {
       pl.hbin[k].vals = cv;
       D.gcf = ws + pl.o_count_gcf;
     }
-    if (pl.hgcf_off[k] != SIZE_MAX) D.gcf = ws + pl.hgcf_off[k];
+    if (pl.hgcf_off[k] != SIZE_MAX) {
+      const auto &c = pl.gcf_copies[pl.hgcf_copy[k]];
+      D.gcf = ws + c.off;
+      D.gcf_real = c.off_real ? (const float *)(ws + c.off_real) : nullptr;
+      D.gcf_imag = c.off_real ? (const int *)(ws + pl.o_gcf_flags) + pl.hgcf_copy[k] : nullptr;
+    }
     if (binned) {
       D.idx = (const int2 *)(ws + pl.o_sidx);
       D.vals = ws + pl.o_svals;
@@ -728,9 +742,15 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
                                   k == 0 ? (int64_t)pl.G * pl.G * maxS * maxS : 0, s));
     }
   }
-  for (const auto &c : pl.gcf_copies)
+  if (!pl.gcf_copies.empty())
+    GG_CUDA(cudaMemsetAsync(ws + pl.o_gcf_flags, 0, sizeof(int) * pl.gcf_copies.size(), s));
+  for (size_t ci = 0; ci < pl.gcf_copies.size(); ++ci) {
+    const auto &c = pl.gcf_copies[ci];
     GG_CUDA(launch_gcf_double_rows(c.src ? c.src : ws + pl.o_count_gcf, ws + c.off, c.S, pl.G,
-                                   c.ntab, (int)vbytes, s));
+                                   c.ntab, (int)vbytes, s,
+                                   c.off_real ? (float *)(ws + c.off_real) : nullptr,
+                                   (int *)(ws + pl.o_gcf_flags) + ci));
+  }
 
   GridLaunch g{};
   g.accum = pl.accum;

@@ -124,9 +124,12 @@ cudaError_t launch_selftest_wait(int *flags, cudaStream_t s);
 bool injected_alloc_failure();
 // Row-doubled copy of ntab consecutive [G*G][S][S] GCF tables for the
 // moving-window kernel: dst[s][b][a] = src[s][b mod S][a] for b < 2S, s over
-// all ntab*G*G sub-kernels (elem_bytes 8 or 16)
+// all ntab*G*G sub-kernels (elem_bytes 8 or 16).  With dst_real (complex64
+// tables only) the real parts are written there too, and *has_imag (zeroed
+// by the caller) is set when any imaginary part is nonzero.
 cudaError_t launch_gcf_double_rows(const void *src, void *dst, int S, int G, int ntab,
-                                   int elem_bytes, cudaStream_t s);
+                                   int elem_bytes, cudaStream_t s,
+                                   float *dst_real = nullptr, int *has_imag = nullptr);
 inline size_t gcf_double_rows_bytes(int S, int G, int elem_bytes) {
   return (size_t)elem_bytes * G * G * 2 * S * S;
 }

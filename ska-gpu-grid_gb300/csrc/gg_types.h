@@ -34,6 +34,10 @@ struct JobDesc {
   // binning key of a visibility is tile * n_gcf + its table index
   const int *gcf_index;  // scatter: the caller's per-visibility indices
   int n_gcf;
+  // moving window, FP32 tables: real parts of the row-doubled tables and a
+  // flag that is nonzero when any imaginary part is (null: not available)
+  const float *gcf_real;
+  const int *gcf_imag;
 };
 
 // A slice of one uv tile's sorted visibilities: the unit of the device work

@@ -88,6 +88,7 @@ template <> struct WinAcc<0> {
   u64 s;
   __device__ __forceinline__ void zero() { s = 0ull; }
   __device__ __forceinline__ void add(u64 t) { s = add2(s, t); }
+  __device__ __forceinline__ void fma(u64 v, u64 g) { s = fma2(v, g, s); }
   __device__ __forceinline__ void into(CellT *c) const {
     const float2 o = *c;
     *c = upk2(add2(pk2(o.x, o.y), s));
@@ -106,6 +107,7 @@ template <> struct WinAcc<1> {
   u64 s;
   __device__ __forceinline__ void zero() { s = 0ull; }
   __device__ __forceinline__ void add(u64 t) { s = add2(s, t); }
+  __device__ __forceinline__ void fma(u64 v, u64 g) { s = fma2(v, g, s); }
   __device__ __forceinline__ void into(CellT *c) const {
     const float4 o = *c;
     u64 e;
@@ -123,6 +125,11 @@ template <> struct WinAcc<2> {
   using CellT = double2;
   double re, im;
   __device__ __forceinline__ void zero() { re = im = 0.0; }
+  // adds v * g for packed FP32 pairs (v complex, g = (r, r) real factor)
+  __device__ __forceinline__ void fma(u64 v, u64 g) {
+    const float2 a = upk2(v), b = upk2(g);
+    add((double)a.x * b.x, (double)a.y * b.x);
+  }
   __device__ __forceinline__ void add(double tr, double ti) {
     re = __dadd_rn(re, tr);
     im = __dadd_rn(im, ti);
@@ -316,6 +323,8 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
     if (leader) issue_next(gfirst + 2);
 
     const VT2 *gtab = reinterpret_cast<const VT2 *>(J.gcf) + (size_t)tab * J.G * J.G * 2 * S * S;
+    // FP32 table without imaginary parts: the real-factor fast path
+    const bool real_tab = !GAUSS && MODE != 2 && J.gcf_real && J.gcf_imag && *J.gcf_imag == 0;
     const int G = J.G;
     // tiles on the border of the grid hold the clamped mains, whose
     // footprints may leave the sub-grid
@@ -409,16 +418,45 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
       // a branch around it), and `nc` says whether it does: same footprint
       // origin and inside `mr`, the chunk end or the run-length limit.
       // Loads run two records ahead of their use.
-      auto step = [&](int r, int mr, const GT (&ga)[Q], const VT2 va, GT (&gc)[Q], VT2 &vc,
-                      bool &nc) {
-        const int r2 = min(r + 2, m - 1);
-        const int2 q = ib[r2];
-        vc = vb[r2];
-        nc = q.x == pkm && r + 2 < mr;
-        load_g(gc, q.y);
-        accum(ga, va);
-      };
-      auto run_interior = [&]() {
+      //
+      // RG: the item's table has no imaginary part (checked on the device
+      // when the row-doubled copy is made): the stages hold the real parts
+      // only (half the table bytes) and a tap is one fused multiply-add of
+      // the complex value by the real factor.
+      auto run_interior = [&](auto real_tag) {
+        constexpr bool RG = decltype(real_tag)::value;
+        using GS = typename std::conditional<RG, float, GT>::type;
+        auto load = [&](GS (&g)[Q], int sub) {
+          if constexpr (RG && MODE != 2) {
+            const float *gp = J.gcf_real + (size_t)tab * J.G * J.G * 2 * S * S +
+                              sub * (2 * S * S) + pofs;
+#pragma unroll
+            for (int k = 0; k < Q; ++k) g[k] = __ldg(gp + k * D * S);
+          } else {
+            load_g(g, sub);
+          }
+        };
+        auto add_rec = [&](const GS (&g)[Q], const VT2 v) {
+          if constexpr (RG && MODE != 2) {
+            const u64 vv = pk2((float)v.x, (float)v.y);
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+              if (S * S % NGT != 0 && !rv[k]) continue;
+              acc[k].fma(vv, pk2(g[k], g[k]));
+            }
+          } else {
+            accum(g, v);
+          }
+        };
+        auto step = [&](int r, int mr, const GS (&ga)[Q], const VT2 va, GS (&gc)[Q], VT2 &vc,
+                        bool &nc) {
+          const int r2 = min(r + 2, m - 1);
+          const int2 q = ib[r2];
+          vc = vb[r2];
+          nc = q.x == pkm && r + 2 < mr;
+          load(gc, q.y);
+          add_rec(ga, va);
+        };
         int r = 0;
         while (r < m) {
           // slow step: record r opens a run
@@ -449,13 +487,13 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
           pkm = pk.x;
           const int r0 = r;
           const int mr = MODE == 1 ? min(m, r0 + (kRunMax - run)) : m;
-          GT ga[Q], gb[Q], gc[Q];
-          load_g(ga, pk.y);
+          GS ga[Q], gb[Q], gc[Q];
+          load(ga, pk.y);
           const int r1 = min(r + 1, m - 1);
           const int2 q = ib[r1];
           vb1 = vb[r1];
           bool nb = q.x == pkm && r + 1 < mr, nc, na;
-          load_g(gb, q.y);
+          load(gb, q.y);
           // fast loop over the rest of the run, three rotating stages
           for (;;) {
             step(r++, mr, ga, va, gc, vc1, nc);
@@ -518,8 +556,18 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
           }
         }
       };
-      if (direct || edge) run_checked();
-      else run_interior();
+      if (direct || edge) {
+        run_checked();
+      } else {
+        // (supports of 16 and more: measured slower for 8, where the per-record
+        // work, not the table loads, dominates)
+        if constexpr (!GAUSS && MODE != 2 && S >= 16) {
+          if (real_tab) run_interior(std::true_type{});
+          else run_interior(std::false_type{});
+        } else {
+          run_interior(std::false_type{});
+        }
+      }
       group_sync(gid, NGT);  // buffer b consumed by the whole group
       if (leader) issue_next(g + 3);
     }
@@ -648,25 +696,35 @@ size_t window_smem_bytes(int S, int accum, int vals_f64, int T, int group_warps,
 
 __global__ void __launch_bounds__(256)
     gcf_double_rows_kernel(const unsigned char *src, unsigned char *dst, int S, int GG,
-                           int elem_bytes) {
+                           int elem_bytes, float *dst_real, int *has_imag) {
   const int64_t per = 2ll * S * S, n = (int64_t)GG * per;
+  bool imag = false;
   for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256) {
     const int64_t sk = i / per;
     const int rem = (int)(i % per), b = rem / S, a = rem % S;
     const int64_t j = (sk * S + (b % S)) * S + a;
-    if (elem_bytes == 16)
+    if (elem_bytes == 16) {
       reinterpret_cast<double2 *>(dst)[i] = reinterpret_cast<const double2 *>(src)[j];
-    else
-      reinterpret_cast<float2 *>(dst)[i] = reinterpret_cast<const float2 *>(src)[j];
+    } else {
+      const float2 v = reinterpret_cast<const float2 *>(src)[j];
+      reinterpret_cast<float2 *>(dst)[i] = v;
+      if (dst_real) {
+        dst_real[i] = v.x;
+        imag |= v.y != 0.f;
+      }
+    }
   }
+  if (imag && has_imag) atomicOr(has_imag, 1);
 }
 
 cudaError_t launch_gcf_double_rows(const void *src, void *dst, int S, int G, int ntab,
-                                   int elem_bytes, cudaStream_t s) {
+                                   int elem_bytes, cudaStream_t s, float *dst_real,
+                                   int *has_imag) {
   const int64_t n = 2ll * ntab * G * G * S * S;
   const int blocks = (int)std::min<int64_t>((n + 255) / 256, 1184);
   gcf_double_rows_kernel<<<blocks, 256, 0, s>>>((const unsigned char *)src, (unsigned char *)dst,
-                                                 S, ntab * G * G, elem_bytes);
+                                                 S, ntab * G * G, elem_bytes,
+                                                 elem_bytes == 8 ? dst_real : nullptr, has_imag);
   count_launch();
   return cudaGetLastError();
 }

@@ -371,6 +371,21 @@ def test_per_visibility_gcf_tables(ctx, mode, prec):
         assert rel_err(planar_from_grid(host, 1, N, False), ref) <= TOL[prec]
 
 
+@pytest.mark.parametrize("imag", [0.0, 1e-3])
+def test_real_and_nearly_real_tables(ctx, imag):
+    """The moving window takes a real-factor path when a table has no
+    imaginary part (detected on the device); a table with a single small
+    imaginary entry must take the complex path.  Both against the oracle."""
+    N, S = 512, 16
+    uv, vals = synth.tracks(N, nant=16, ntime=2000, npts=None, seed=77)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    gcf[27, 7, 9] += np.complex64(1j * imag)
+    o = opts_for("window", "cc_comp", layout=gg.LAYOUT_INTERLEAVED)
+    got, flags = run(ctx, o, uv, vals, gcf, N, S, "cc_comp")
+    assert flags == [0, 0, 0, 0]
+    assert rel_err(got, oracle_for(uv, vals, gcf, N, S)) <= TOL["cc_comp"]
+
+
 def test_per_visibility_gcf_rejected_by_gather(ctx):
     N, S = 64, 8
     d = [torch.zeros((10, 2), dtype=torch.float64, device="cuda"),
