@@ -105,6 +105,27 @@ def pairs(c):
     return np.stack([c.real, c.imag], -1).astype(np.float64)
 
 
+class nvtx_range:
+    """an NVTX range around a region (a profiler can select the launches in
+    it: ncu --nvtx --nvtx-include "gg_profiled/"); a no-op without NVTX"""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __enter__(self):
+        try:
+            import torch
+            torch.cuda.nvtx.range_push(self.name)
+            self.on = True
+        except Exception:
+            self.on = False
+
+    def __exit__(self, *exc):
+        if self.on:
+            import torch
+            torch.cuda.nvtx.range_pop()
+
+
 def max_over_ranks(x, dist, dev=None):
     """the largest value of x over all ranks (x unchanged without a process
     group): every rank's timed region ends when the slowest rank's does"""
@@ -269,10 +290,10 @@ def cpu_rate(jobs, budget_s, threads=None):
 # ---------------------------------------------------------------------------
 # shared pieces of the batched and served workloads
 # ---------------------------------------------------------------------------
-def stream_inputs(n, seed):
+def stream_inputs(n, seed, nsets=8):
     import synth
-    pools = synth.track_pool(seed=seed)
-    specs = synth.request_specs(n, seed=seed + 1)
+    pools = synth.track_pool(seed=seed, nsets=nsets)
+    specs = synth.request_specs(n, seed=seed + 1, nsets=nsets)
     gcfs = {S: synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64) for S in (8, 16)}
     return pools, specs, gcfs
 
@@ -456,7 +477,8 @@ def run_served(args, rank, world, local_rank, dist):
         jobs.append(j)
     for _ in range(3):
         ctx.grid_batch(opts, jobs)
-    ctx.grid_batch(opts, jobs)
+    with nvtx_range("gg_profiled"):
+        ctx.grid_batch(opts, jobs)
     _, kern_ms, _ = ctx.profile_last()
     nv = sum(j.npts for j in jobs)
     alg = nv * 16 + sum(2 * 8 * j.img_dim * j.img_dim for j in jobs)
@@ -583,7 +605,11 @@ def run_batch(args, rank, world, local_rank, dist):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     n = w["n"]
-    pools, specs, gcfs = stream_inputs(n, seed=17 + rank)
+    if args.profile_small:
+        # a small case of the same kernel for detailed profiler captures:
+        # 64 jobs from 2 observations per grid side (about 1.5 GB on the device)
+        n = 64
+    pools, specs, gcfs = stream_inputs(n, seed=17 + rank, nsets=2 if args.profile_small else 8)
     total_vis = int(specs["nvis"].sum())
     dp = DevicePools(pools, dev)
     dg = {S: torch.from_numpy(gcfs[S].reshape(-1)).to(dev) for S in (8, 16)}
@@ -663,7 +689,8 @@ def run_batch(args, rank, world, local_rank, dist):
         plain[label] = round(total_vis / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
     ctx.profile(True)
     ctx.grid_batch(opts, jobs)
-    ctx.grid_batch(opts, jobs)
+    with nvtx_range("gg_profiled"):
+        ctx.grid_batch(opts, jobs)
     _, kern_ms, _ = ctx.profile_last()
     alg = total_vis * 16 + sum(2 * 8 * j.img_dim * j.img_dim for j in jobs)
     taps = sum(j.npts * j.gcf_dim * j.gcf_dim for j in jobs)
@@ -838,7 +865,8 @@ def run_single(args, rank, world, local_rank, dist):
         for k in range(args.steps):
             flush.fill_(k & 0xff)            # evict L2 (untimed)
             start[k].record(stream)
-            ctx.grid(o, out, d_uv, d_vals, d_gcf, N, S)
+            with nvtx_range("gg_profiled" if k == args.steps - 1 else "gg_step"):
+                ctx.grid(o, out, d_uv, d_vals, d_gcf, N, S)
             end[k].record(stream)
             b, g_ms, _ = ctx.profile_last()
             kern_ms.append(g_ms)
@@ -991,6 +1019,9 @@ def main():
                     help="seconds of CPU gridding for the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--profile-small", action="store_true",
+                    help="batch256: 64 jobs from 2 observations per grid side, a case small "
+                         "enough for multi-pass profiler captures")
     ap.add_argument("--method", choices=["scatter", "gather", "window"], default=None,
                     help="single-job workloads: grid with this method instead of the "
                          "workload's own")
