@@ -182,7 +182,9 @@ __host__ __device__ constexpr int win_default_warps(int S) {
 template <int S, int W> struct WinCfg {
   static constexpr int NGT = 32 * W;                         // threads per group
   static constexpr int Q = (S * S + NGT - 1) / NGT;          // residues per thread
-  static constexpr int K = S >= 32 ? 512 : (S >= 16 ? 256 : 128);  // records per chunk
+  // records per chunk (staging buffers); 128 for S=16 keeps two CTAs' shared
+  // memory under the 164 KB carveout, leaving 92 KB of L1 for the GCF table
+  static constexpr int K = S >= 32 ? 512 : 128;
   static constexpr int GROUPS = kWinThreads / NGT;
   // resident CTAs per SM the register allocation is held to (shared memory
   // allows as many at the default tile sizes)
