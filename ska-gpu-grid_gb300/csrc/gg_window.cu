@@ -22,13 +22,23 @@
 //    component, updated with Knuth's TwoSum on the packed (re, im) pair
 //    (f32x2 instructions) whenever a register run is added in; register runs
 //    are cut after kRunMax records, which bounds their plain-FP32 error.
-//  * Visibility records (packed indices + values) stream through shared
-//    memory by 1-D TMA bulk copies, double-buffered, as one continuous stream
-//    across work items (the next item is claimed early and its first chunk
-//    prefetched while the current one is gridded).
+//  * Visibility records (both main cells in one word + the sub-kernel index,
+//    and the values) stream through shared memory by 1-D TMA bulk copies,
+//    double-buffered, as one continuous stream across work items (the next
+//    item is claimed early and its first chunk prefetched while the current
+//    one is gridded).
+//  * Records come in runs with an unchanged footprint origin.  The first
+//    record of a run works out the target cells and flushes the register
+//    sums whose cell changed; the rest of the run goes through a fast loop
+//    that only loads GCF values (two records ahead of their use, at fixed
+//    strides in a row-doubled copy of the table) and accumulates.  Tables
+//    without imaginary parts (flagged on the device) take a real-factor
+//    variant for supports of 16 and more.
 //  * Once per item the sub-grid is flushed to HBM with native vector
 //    reductions (touched cells only) and zeroed as it is read.  Items too
-//    sparse to pay for that flush send each register sum straight to HBM.
+//    sparse to pay for that flush, and edge tiles (whose clamped mains may
+//    reach outside the sub-grid), take a bounds-checked one-stage loop; the
+//    sparse ones send each register sum straight to HBM.
 #include <algorithm>
 #include <climits>
 #include <type_traits>
