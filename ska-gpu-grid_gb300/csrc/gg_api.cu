@@ -229,6 +229,30 @@ struct Plan {
   char *ws = nullptr;      // workspace the addresses are bound to
 };
 
+// Side stream of a moving-window launch: the output grids are zeroed there
+// while the binning and the earlier support classes run on the main stream
+// (the window kernels are issue bound and leave HBM nearly idle); each class
+// waits only for the zeroing of its own grids.
+struct AuxStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t done[kMaxClasses] = {};
+  int init() {
+    GG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    GG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    for (auto &e : done) GG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return GG_OK;
+  }
+  void release() {
+    for (auto &e : done)
+      if (e) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (s) cudaStreamDestroy(s);
+    s = nullptr;
+    fork = nullptr;
+  }
+};
+
 struct gg_context {
   int device = 0;
   int sm_count = 152;
@@ -239,6 +263,7 @@ struct gg_context {
   cudaEvent_t upload_done = nullptr;  // staging may be rewritten after this
   cudaEvent_t exec_done = nullptr;    // workspace free after this
   cudaStream_t own = nullptr;         // stream of the host-path calls
+  AuxStream aux;                      // zeroing beside moving-window launches
   // host-path device copies of the caller's buffers
   DevBuf h_uv, h_vals, h_gcf, h_out;
   Plan plan;
@@ -257,6 +282,7 @@ static int ctx_init(gg_context *c, int device) {
   GG_CUDA(cudaEventCreateWithFlags(&c->upload_done, cudaEventDisableTiming));
   GG_CUDA(cudaEventCreateWithFlags(&c->exec_done, cudaEventDisableTiming));
   GG_CUDA(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking));
+  if (int st = c->aux.init()) return st;
   for (auto &e : c->prof) GG_CUDA(cudaEventCreate(&e));
   int st = c->flags.ensure(64 * sizeof(int));
   if (st) return st;
@@ -279,6 +305,7 @@ static void ctx_release(gg_context *c) {
   for (auto &e : c->prof)
     if (e) cudaEventDestroy(e);
   if (c->own) cudaStreamDestroy(c->own);
+  c->aux.release();
 }
 
 // GG_MODE_AUTO: the moving window for FP32 values (fastest at every size
@@ -714,7 +741,7 @@ struct ProfEvents {
 // or synchronises -- the sequence can be captured into a CUDA graph.
 static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int sm_count,
                         cudaStream_t s, const void *upload, cudaEvent_t upload_ev,
-                        const ProfEvents *prof) {
+                        const ProfEvents *prof, const AuxStream *aux) {
   char *ws = pl.ws;
   if (prof) GG_CUDA(cudaEventRecord(prof->ev[0], s));
   if (upload) {
@@ -727,7 +754,22 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
   const int *dclass = (const int *)(ws + pl.o_class);
   const size_t vbytes = pl.vals_f64 ? 16 : 8;
 
-  for (auto &z : pl.zero_ranges) GG_CUDA(cudaMemsetAsync(z.first, 0, z.second, s));
+  // output zeroing: on the side stream, class by class, for the moving
+  // window (jobs are in class order, one zero range each); else here
+  const bool side = aux && aux->s && pl.mode == GG_MODE_WINDOW &&
+                    pl.zero_ranges.size() == (size_t)pl.njobs &&
+                    pl.classes.size() <= (size_t)kMaxClasses;
+  if (side) {
+    GG_CUDA(cudaEventRecord(aux->fork, s));
+    GG_CUDA(cudaStreamWaitEvent(aux->s, aux->fork, 0));
+    for (size_t ci = 0; ci < pl.classes.size(); ++ci) {
+      for (int j = pl.classes[ci].j0; j < pl.classes[ci].j1; ++j)
+        GG_CUDA(cudaMemsetAsync(pl.zero_ranges[j].first, 0, pl.zero_ranges[j].second, aux->s));
+      GG_CUDA(cudaEventRecord(aux->done[ci], aux->s));
+    }
+  } else {
+    for (auto &z : pl.zero_ranges) GG_CUDA(cudaMemsetAsync(z.first, 0, z.second, s));
+  }
   if (pl.comp_lo) {
     size_t lo_bytes = pl.ws_bytes - pl.o_lo;
     GG_CUDA(cudaMemsetAsync(ws + pl.o_lo, 0, lo_bytes, s));
@@ -808,6 +850,7 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
       g.group_warps = cl.W;
       g.items = items + ci * pl.class_cap;
       g.nitems = flags + 8 + ci;
+      if (side) GG_CUDA(cudaStreamWaitEvent(s, aux->done[ci], 0));
       g.item_next = flags + 12 + ci;
       g.max_items = pl.class_cap;
       GG_CUDA(launch_window(g, s));
@@ -863,7 +906,7 @@ static int enqueue_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs
   ProfEvents pe;
   for (int i = 0; i < 4; ++i) pe.ev[i] = c->prof[i];
   st = plan_enqueue(opt, pl, (int *)c->flags.p, c->sm_count, s, c->staging.p,
-                    c->upload_done, c->profile ? &pe : nullptr);
+                    c->upload_done, c->profile ? &pe : nullptr, &c->aux);
   if (st) return st;
   if (c->profile) c->prof_recorded = 1;
   GG_CUDA(cudaEventRecord(c->exec_done, s));
@@ -1150,6 +1193,7 @@ struct gg_plan {
   gg_options opt;
   Plan pl;
   DevBuf ws, flags;
+  AuxStream aux;
 };
 
 extern "C" {
@@ -1176,6 +1220,12 @@ int gg_plan_create(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
     p->ws.release();
     return st;
   }
+  if ((st = p->aux.init())) {
+    p->ws.release();
+    p->flags.release();
+    p->aux.release();
+    return st;
+  }
   std::vector<char> tables(p->pl.table_bytes);
   plan_bind(opt, p->pl, (char *)p->ws.p, tables.data());
   cudaError_t e = cudaMemcpy(p->ws.p, tables.data(), p->pl.table_bytes, cudaMemcpyHostToDevice);
@@ -1183,6 +1233,7 @@ int gg_plan_create(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
   if (e != cudaSuccess) {
     p->ws.release();
     p->flags.release();
+    p->aux.release();
     return cuda_fail(e, "plan upload");
   }
   *out = p.release();
@@ -1193,7 +1244,7 @@ int gg_plan_launch(gg_plan *p, void *stream) {
   if (!p) return fail(GG_ERR_ARG, "plan: null");
   GG_CUDA(cudaSetDevice(p->ctx->device));
   return plan_enqueue(&p->opt, p->pl, (int *)p->flags.p, p->ctx->sm_count,
-                      (cudaStream_t)stream, nullptr, nullptr, nullptr);
+                      (cudaStream_t)stream, nullptr, nullptr, nullptr, &p->aux);
 }
 
 int gg_plan_read_flags(gg_plan *p, void *stream, int32_t flags[4]) {
@@ -1215,6 +1266,7 @@ int gg_plan_destroy(gg_plan *p) {
   cudaDeviceSynchronize();
   p->ws.release();
   p->flags.release();
+  p->aux.release();
   delete p;
   return GG_OK;
 }
