@@ -337,6 +337,8 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
     const VT2 *gtab = reinterpret_cast<const VT2 *>(J.gcf) + (size_t)tab * J.G * J.G * 2 * S * S;
     // FP32 table without imaginary parts: the real-factor fast path
     const bool real_tab = !GAUSS && MODE != 2 && J.gcf_real && J.gcf_imag && *J.gcf_imag == 0;
+    const float *const greal =
+        real_tab ? J.gcf_real + (size_t)tab * J.G * J.G * 2 * S * S : nullptr;
     const int G = J.G;
     // tiles on the border of the grid hold the clamped mains, whose
     // footprints may leave the sub-grid
@@ -440,8 +442,7 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
         using GS = typename std::conditional<RG, float, GT>::type;
         auto load = [&](GS (&g)[Q], int sub) {
           if constexpr (RG && MODE != 2) {
-            const float *gp = J.gcf_real + (size_t)tab * J.G * J.G * 2 * S * S +
-                              sub * (2 * S * S) + pofs;
+            const float *gp = greal + sub * (2 * S * S) + pofs;
 #pragma unroll
             for (int k = 0; k < Q; ++k) g[k] = __ldg(gp + k * D * S);
           } else {
