@@ -33,7 +33,7 @@
 //    that only loads GCF values (two records ahead of their use, at fixed
 //    strides in a row-doubled copy of the table) and accumulates.  Tables
 //    without imaginary parts (flagged on the device) take a real-factor
-//    variant for supports of 16 and more.
+//    variant.
 //  * Once per item the sub-grid is flushed to HBM with native vector
 //    reductions (touched cells only) and zeroed as it is read.  Items too
 //    sparse to pay for that flush, and edge tiles (whose clamped mains may
@@ -572,9 +572,7 @@ __global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
       if (direct || edge) {
         run_checked();
       } else {
-        // (supports of 16 and more: measured slower for 8, where the per-record
-        // work, not the table loads, dominates)
-        if constexpr (!GAUSS && MODE != 2 && S >= 16) {
+        if constexpr (!GAUSS && MODE != 2) {
           if (real_tab) run_interior(std::true_type{});
           else run_interior(std::false_type{});
         } else {
