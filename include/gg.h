@@ -91,7 +91,11 @@ typedef struct gg_options {
                             window_chunk all 0: 1 = pick them per support
                             class by timing candidates on the first batch of
                             each size class (that call synchronises its
-                            stream), then reuse the choice (process-wide)   */
+                            stream), then reuse the choice (process-wide).
+                            The trials grid the batch itself (writing its
+                            outputs, which the real launch then rewrites);
+                            gg_plan_create runs them at creation, on the
+                            inputs present then.                           */
   int32_t reserved[5];
 } gg_options;
 
