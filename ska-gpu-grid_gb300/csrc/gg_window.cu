@@ -192,13 +192,12 @@ __host__ __device__ constexpr int win_default_warps(int S) {
 template <int S, int W> struct WinCfg {
   static constexpr int NGT = 32 * W;                         // threads per group
   static constexpr int Q = (S * S + NGT - 1) / NGT;          // residues per thread
-  // records per chunk (staging buffers); 128 for S=16 keeps two CTAs' shared
-  // memory under the 164 KB carveout, leaving 92 KB of L1 for the GCF table
-  static constexpr int K = S >= 32 ? 512 : 128;
+  // records per chunk (staging buffers); 64 for S=16 lets three CTAs' shared
+  // memory (3 x 70 KB) fit an SM, which measured faster than two CTAs with
+  // more L1 left for the GCF table
+  static constexpr int K = S >= 32 ? 512 : (S >= 16 ? 64 : 128);
   static constexpr int GROUPS = kWinThreads / NGT;
-  // resident CTAs per SM the register allocation is held to (shared memory
-  // allows as many at the default tile sizes)
-  static constexpr int MIN_CTAS = S <= 8 ? 3 : (S <= 16 ? 2 : 1);
+
 };
 
 template <int S, int W, int MODE, bool GAUSS>
@@ -228,8 +227,18 @@ __device__ __forceinline__ void group_sync(int gid, int nthreads) {
   }
 }
 
+// Resident CTAs per SM the register allocation is held to: as many as the
+// shared memory of the configuration allows at the default tile (16), where
+// the compiler then fits the loop without spilling; FP64 sums get one fewer.
+__host__ __device__ constexpr int win_min_ctas(int S, int W, int MODE) {
+  return S <= 4 ? 2
+         : S <= 8 ? (W == 1 ? 2 : (MODE == 2 ? 3 : 4))
+         : S <= 16 ? (W == 1 ? 1 : (MODE == 2 ? 2 : 3))
+                   : 1;
+}
+
 template <int S, int W, int MODE, bool GAUSS>
-__global__ void __launch_bounds__(kWinThreads, WinCfg<S, W>::MIN_CTAS)
+__global__ void __launch_bounds__(kWinThreads, win_min_ctas(S, W, MODE))
     window_kernel(KParams kp) {
   using Cfg = WinCfg<S, W>;
   using L = WinLayout<S, W, MODE, GAUSS>;
