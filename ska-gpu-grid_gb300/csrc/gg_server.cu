@@ -19,6 +19,7 @@
 //  * latency is measured from a request's arrival (its submit time, or its
 //    scheduled time in a trace) to that completion.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -80,7 +81,14 @@ struct gg_server {
   std::vector<int64_t> gcf_dim;
   std::vector<int> gcf_type;
   std::thread sched;
-  std::vector<std::thread> feeders;
+  // arrival-trace feeders; a finished one sets its flag and is joined by the
+  // next gg_server_submit_schedule (or at destruction)
+  struct Feeder {
+    std::thread t;
+    std::shared_ptr<std::atomic<bool>> finished;
+  };
+  std::vector<Feeder> feeders;
+  std::mutex feeders_mu;  // guards `feeders` (client threads)
   int feeders_running = 0;
   // statistics
   int64_t n_submitted = 0, n_completed = 0, n_failed = 0, n_rejected = 0,
@@ -443,7 +451,18 @@ int gg_server_submit_schedule(gg_server *srv, const gg_request *reqs,
             [](const std::pair<double, Req *> &a, const std::pair<double, Req *> &b) {
               return a.first < b.first;
             });
-  srv->feeders.emplace_back([srv, plan]() {
+  // join the feeders of earlier traces that have finished
+  std::lock_guard<std::mutex> flk(srv->feeders_mu);
+  for (auto it = srv->feeders.begin(); it != srv->feeders.end();) {
+    if (it->finished->load()) {
+      it->t.join();
+      it = srv->feeders.erase(it);
+    } else {
+      ++it;
+    }
+  }
+  auto finished = std::make_shared<std::atomic<bool>>(false);
+  std::thread feeder([srv, plan, finished]() {
     for (const auto &e : plan) {
       const auto when = srv->epoch + std::chrono::duration_cast<Clock::duration>(
                                          std::chrono::duration<double>(e.first));
@@ -463,7 +482,9 @@ int gg_server_submit_schedule(gg_server *srv, const gg_request *reqs,
     std::lock_guard<std::mutex> lk(srv->mu);
     --srv->feeders_running;
     srv->cv_sched.notify_one();
+    finished->store(true);
   });
+  srv->feeders.push_back({std::move(feeder), finished});
   return GG_OK;
 }
 
@@ -593,7 +614,10 @@ int gg_server_destroy(gg_server *srv) {
     srv->cv_sched.notify_all();
     srv->cv_feed.notify_all();
   }
-  for (auto &t : srv->feeders) t.join();
+  {
+    std::lock_guard<std::mutex> flk(srv->feeders_mu);
+    for (auto &f : srv->feeders) f.t.join();
+  }
   {
     std::lock_guard<std::mutex> lk(srv->mu);
     srv->cv_sched.notify_all();
