@@ -70,6 +70,13 @@ extern "C" {
                              x = a - sub/G, evaluated on the device          */
 #define GG_GCF_COUNT 2    /* DEBUG1 footprint mode (Defines.h:78): every tap
                              adds (1, visibility index)                     */
+#define GG_GCF_WPHASE 3   /* COMPUTE_GCF as the reference's scatter kernel
+                             computes it (grid_gpu.cu:103-108, 137-147):
+                             every tap of a visibility gets (sin p, cos p),
+                             p = p1 - p2*sqrt(dx^2 + dy^2) in FP32 with
+                             p1 = 2*pi*w, p2 = p1*T, (T, w) = the table entry
+                             at the centre offset S(S-1)/2-1 and dx = main_x
+                             - u + sub_x/G; gridded by the scatter method   */
 
 typedef struct gg_options {
   int32_t mode;          /* GG_MODE_*                                        */

@@ -9,7 +9,8 @@
  * The reference picks its method with compile-time macros; they are honoured
  * here the same way and turned into gg_options:
  *   __GATHER -> GG_MODE_GATHER, __MOVING_WINDOW -> GG_MODE_WINDOW,
- *   __COMPUTE_GCF -> GG_GCF_GAUSSIAN, POLARIZATIONS, GCF_GRID.
+ *   __COMPUTE_GCF -> GG_GCF_WPHASE (the reference scatter kernel's factor),
+ *   POLARIZATIONS, GCF_GRID.
  * Differences from the reference (all deliberate): errors are returned by
  * gg_last_status() instead of only printed, nothing is allocated or pinned
  * per call, and the instantiation set is the same three type pairs
@@ -41,7 +42,7 @@ inline gg_options options_from_macros() {
   o.mode = GG_MODE_WINDOW;
 #endif
 #if defined(__COMPUTE_GCF)
-  o.gcf_kind = GG_GCF_GAUSSIAN;
+  o.gcf_kind = GG_GCF_WPHASE;
 #endif
 #if defined(POLARIZATIONS)
   o.polarizations = POLARIZATIONS;

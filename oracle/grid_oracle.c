@@ -30,7 +30,28 @@ typedef struct {
   long y0, y1; /* rows owned by this worker: [y0, y1) */
   const int32_t *gcfinx; /* per-visibility table index (NULL: table 0) */
   int n_gcf;
+  int wphase; /* COMPUTE_GCF phase factor instead of the table */
 } band_job;
+
+/* The reference GPU scatter kernel's COMPUTE_GCF factor (grid_gpu.cu:103-108,
+ * 137-147): (T, w) = the first entry of the centre-offset table; every tap of
+ * a visibility gets (sin phi, cos phi), phi = p1 - p2*sqrt(dx^2 + dy^2) with
+ * dx = main_x - u + sub_x/G evaluated in double and stored as float, the
+ * rest in float.  It has no CPU counterpart in the reference; this is its
+ * restatement for the checker. */
+static void wphase_factor(double u, double v, int main_x, int sub_x, int main_y,
+                          int sub_y, int G, double T, double w, double *r2,
+                          double *i2) {
+  const float p1 = (float)(2 * 3.1415926 * w);
+  const float p2 = (float)((double)p1 * T);
+  float xs = (float)((double)main_x - u + sub_x * 1.0 / G);
+  float ys = (float)((double)main_y - v + sub_y * 1.0 / G);
+  xs = xs * xs;
+  ys = ys * ys;
+  const float ph = p1 - p2 * sqrtf(xs + ys);
+  *r2 = (double)sinf(ph);
+  *i2 = (double)cosf(ph);
+}
 
 /* Body of gridCPU_pz (grid.cu:157-191), restricted to rows [y0, y1).  The
  * tap loops run a (then b) from S/2 down to -S/2+1 (grid.cu:167-168); each
@@ -56,12 +77,17 @@ static void grid_band(const band_job *j) {
       table = (long)j->gcfinx[n] * G * G * S * S;
     }
     const double *g = gcf + 2 * (table + S * S * ((long)G * sub_y + sub_x));
+    double wr = 0, wi = 0;
+    if (j->wphase)
+      wphase_factor(j->uv[2 * n], j->uv[2 * n + 1], main_x, sub_x, main_y, sub_y, G, gcf[0],
+                    gcf[1], &wr, &wi);
     for (long a = S / 2; a > -S / 2; a--)
       for (long b = S / 2; b > -S / 2; b--) {
         long x = main_x + a, y = main_y + b;
         if (x < 0 || y < 0 || x >= N || y >= N) continue;
         if (y < j->y0 || y >= j->y1) continue;
-        double r2 = g[2 * (S * b + a)], i2 = g[2 * (S * b + a) + 1];
+        double r2 = j->wphase ? wr : g[2 * (S * b + a)];
+        double i2 = j->wphase ? wi : g[2 * (S * b + a) + 1];
         for (int p = 0; p < P; p++) {
           size_t cell = (size_t)x + (size_t)N * y + (size_t)p * N * N;
           if (j->debug1) {
@@ -82,7 +108,7 @@ void oracle_grid_pz(double *out_planar, const double *uv, const double *vals,
                     size_t npts, size_t img_dim, const double *gcf,
                     size_t gcf_dim, int gcf_grid, int pols, int debug1) {
   band_job j = {out_planar, uv, vals, gcf, npts, img_dim, gcf_dim,
-                gcf_grid, pols, debug1, 0, (long)img_dim, NULL, 1};
+                gcf_grid, pols, debug1, 0, (long)img_dim, NULL, 1, 0};
   grid_band(&j);
 }
 
@@ -99,11 +125,32 @@ void oracle_grid_pz_mt(double *out_planar, const double *uv,
                         gcf_dim, gcf_grid, pols, debug1, nthreads);
 }
 
+static void grid_mt(double *out_planar, const double *uv, const double *vals,
+                    const int32_t *gcfinx, size_t npts, size_t img_dim,
+                    const double *gcf, int n_gcf, size_t gcf_dim, int gcf_grid,
+                    int pols, int debug1, int wphase, int nthreads);
+
 void oracle_grid_pz_gcfinx(double *out_planar, const double *uv,
                            const double *vals, const int32_t *gcfinx,
                            size_t npts, size_t img_dim, const double *gcf,
                            int n_gcf, size_t gcf_dim, int gcf_grid, int pols,
                            int debug1, int nthreads) {
+  grid_mt(out_planar, uv, vals, gcfinx, npts, img_dim, gcf, n_gcf, gcf_dim, gcf_grid, pols,
+          debug1, 0, nthreads);
+}
+
+void oracle_grid_pz_wphase(double *out_planar, const double *uv,
+                           const double *vals, size_t npts, size_t img_dim,
+                           const double *gcf, size_t gcf_dim, int gcf_grid,
+                           int pols, int nthreads) {
+  grid_mt(out_planar, uv, vals, NULL, npts, img_dim, gcf, 1, gcf_dim, gcf_grid, pols, 0, 1,
+          nthreads);
+}
+
+static void grid_mt(double *out_planar, const double *uv, const double *vals,
+                    const int32_t *gcfinx, size_t npts, size_t img_dim,
+                    const double *gcf, int n_gcf, size_t gcf_dim, int gcf_grid,
+                    int pols, int debug1, int wphase, int nthreads) {
   if (nthreads < 1) nthreads = 1;
   if ((size_t)nthreads > img_dim) nthreads = (int)img_dim;
   band_job *jobs = (band_job *)calloc((size_t)nthreads, sizeof(band_job));
@@ -113,7 +160,7 @@ void oracle_grid_pz_gcfinx(double *out_planar, const double *uv,
                   gcf_grid, pols, debug1,
                   (long)(img_dim * (size_t)t / (size_t)nthreads),
                   (long)(img_dim * (size_t)(t + 1) / (size_t)nthreads),
-                  gcfinx, n_gcf};
+                  gcfinx, n_gcf, wphase};
     jobs[t] = j;
   }
   char *joined = (char *)calloc((size_t)nthreads, 1);

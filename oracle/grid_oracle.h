@@ -53,6 +53,17 @@ void oracle_grid_pz_gcfinx(double *out_planar, const double *uv,
                            int n_gcf, size_t gcf_dim, int gcf_grid, int pols,
                            int debug1, int nthreads);
 
+/* gridCPU_pz with the reference GPU scatter kernel's COMPUTE_GCF factor in
+ * place of the table (grid_gpu.cu:103-108, 137-147): every tap of a
+ * visibility is multiplied by (sin phi, cos phi), phi computed in float from
+ * (T, w) = the first entry of the centre-offset table gcf (gcf itself is
+ * passed un-offset, as everywhere here) and the visibility's sub-pixel
+ * position. */
+void oracle_grid_pz_wphase(double *out_planar, const double *uv,
+                           const double *vals, size_t npts, size_t img_dim,
+                           const double *gcf, size_t gcf_dim, int gcf_grid,
+                           int pols, int nthreads);
+
 /* The index step of gridCPU_pz (grid.cu:159-163): main = floor(u),
  * sub = floorf(G*(u - floorf(u))) with the float conversions C applies.
  * Writes packed (main*G+sub) pairs like vis2ints (grid_gpu.cu:352-365). */

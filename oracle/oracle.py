@@ -53,6 +53,8 @@ def lib():
         L.oracle_grid_pz_gcfinx.argtypes = [_dp, _dp, _dp, _ip, _sz, _sz, _dp, ctypes.c_int,
                                             _sz, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int]
+        L.oracle_grid_pz_wphase.argtypes = [_dp, _dp, _dp, _sz, _sz, _dp, _sz, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_int]
         L.oracle_vis2ints.argtypes = [_dp, _sz, ctypes.c_int, _ip]
         L.oracle_vis2ints_gpu_formula.argtypes = [_dp, _sz, ctypes.c_int, _ip]
         L.oracle_set_bookmarks.argtypes = [_ip, _sz, ctypes.c_int, ctypes.c_int,
@@ -61,6 +63,7 @@ def lib():
                                           ctypes.c_double]
         L.oracle_gcf_from_1d.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int]
         for f in (L.oracle_grid_pz, L.oracle_grid_pz_mt, L.oracle_grid_pz_gcfinx,
+                  L.oracle_grid_pz_wphase,
                   L.oracle_vis2ints,
                   L.oracle_vis2ints_gpu_formula, L.oracle_set_bookmarks,
                   L.oracle_gaussian_gcf, L.oracle_gcf_from_1d):
@@ -117,6 +120,21 @@ def grid_pz_gcfinx(uv, vals, gcfinx, gcfs, img_dim: int, gcf_dim: int, pols: int
     out = np.zeros((2, pols, img_dim, img_dim), np.float64)
     lib().oracle_grid_pz_gcfinx(_ptr(out), _ptr(uv), _ptr(vals), _ptr(idx, _ip), npts, img_dim,
                                 _ptr(tabs), n_gcf, gcf_dim, gcf_grid, pols, 0, max(1, nthreads))
+    return out
+
+
+def grid_pz_wphase(uv, vals, gcf, img_dim: int, gcf_dim: int, pols: int = 1,
+                   gcf_grid: int = 8, nthreads: int = 1) -> np.ndarray:
+    """gridCPU_pz with the reference scatter kernel's COMPUTE_GCF factor: every
+    tap of a visibility gets (sin phi, cos phi), (T, w) taken from the entry
+    S(S-1)/2-1 of ``gcf``.  Returns (2, P, N, N)."""
+    uv = _as_pairs(uv)
+    vals = _as_pairs(vals)
+    gcf = _as_pairs(gcf)
+    npts = uv.shape[0]
+    out = np.zeros((2, pols, img_dim, img_dim), np.float64)
+    lib().oracle_grid_pz_wphase(_ptr(out), _ptr(uv), _ptr(vals), npts, img_dim, _ptr(gcf),
+                                gcf_dim, gcf_grid, pols, max(1, nthreads))
     return out
 
 

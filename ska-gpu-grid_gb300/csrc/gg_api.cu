@@ -158,7 +158,7 @@ static int check_options(const gg_options *o) {
     return fail(GG_ERR_ARG, "options: layout %d unknown", o->layout);
   if (o->accum != GG_ACC_PLAIN && o->accum != GG_ACC_COMPENSATED)
     return fail(GG_ERR_ARG, "options: accum %d unknown", o->accum);
-  if (o->gcf_kind < GG_GCF_TABLE || o->gcf_kind > GG_GCF_COUNT)
+  if (o->gcf_kind < GG_GCF_TABLE || o->gcf_kind > GG_GCF_WPHASE)
     return fail(GG_ERR_ARG, "options: gcf_kind %d unknown", o->gcf_kind);
   if (!is_pow2(o->oversample) || o->oversample > 64)
     return fail(GG_ERR_ARG, "options: oversample %d must be a power of two <= 64",
@@ -314,6 +314,8 @@ static void ctx_release(gg_context *c) {
 // the window kernel is slower on this GPU than FP64 L2 reductions (1024^2,
 // S=16: 399 vs 218 Mvis/s)
 static int resolve_mode(const gg_options *o, int S, int vals_f64) {
+  // the COMPUTE_GCF phase factor is the reference scatter kernel's: scatter
+  if (o->gcf_kind == GG_GCF_WPHASE) return GG_MODE_SCATTER;
   if (o->mode != GG_MODE_AUTO) return o->mode;
   (void)S;
   return vals_f64 ? GG_MODE_SCATTER : GG_MODE_WINDOW;
@@ -479,8 +481,8 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
     if (!J.out) return fail(GG_ERR_ARG, "job %d: out is null", j);
     if (J.npts > 0 && (!J.uv || !J.vals))
       return fail(GG_ERR_ARG, "job %d: uv/vals null", j);
-    if (opt->gcf_kind == GG_GCF_TABLE && !J.gcf)
-      return fail(GG_ERR_ARG, "job %d: TABLE GCF needs gcf", j);
+    if ((opt->gcf_kind == GG_GCF_TABLE || opt->gcf_kind == GG_GCF_WPHASE) && !J.gcf)
+      return fail(GG_ERR_ARG, "job %d: TABLE and WPHASE GCFs need gcf", j);
     if (J.gcf_index) {
       if (opt->gcf_kind != GG_GCF_TABLE)
         return fail(GG_ERR_ARG, "job %d: gcf_index needs a TABLE GCF", j);
@@ -798,6 +800,7 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
   g.accum = pl.accum;
   g.vals_f64 = pl.vals_f64;
   g.gauss = pl.gauss;
+  g.wphase = opt->gcf_kind == GG_GCF_WPHASE;
   g.sigma = pl.sigma;
   g.G = pl.G;
   g.tile = pl.T;
@@ -1419,7 +1422,8 @@ extern "C" int gg_grid_host(const gg_options *opt, int out_type, void *out,
   if (st) return st;
   if (!out) return fail(GG_ERR_ARG, "out: null");
   if (npts > 0 && (!uv || !vals)) return fail(GG_ERR_ARG, "in/in_vals: null");
-  if (opt->gcf_kind == GG_GCF_TABLE && !gcf) return fail(GG_ERR_ARG, "gcf: null");
+  if ((opt->gcf_kind == GG_GCF_TABLE || opt->gcf_kind == GG_GCF_WPHASE) && !gcf)
+    return fail(GG_ERR_ARG, "gcf: null");
   gg_context *c = nullptr;
   if ((st = host_ctx(&c))) return st;
   std::lock_guard<std::mutex> lk(c->mu);
@@ -1442,7 +1446,7 @@ extern "C" int gg_grid_host(const gg_options *opt, int out_type, void *out,
     GG_CUDA(cudaMemcpyAsync(c->h_uv.p, uv, uvb * npts, cudaMemcpyHostToDevice, s));
     GG_CUDA(cudaMemcpyAsync(c->h_vals.p, vals, vb * P * npts, cudaMemcpyHostToDevice, s));
   }
-  if (opt->gcf_kind == GG_GCF_TABLE)
+  if (opt->gcf_kind == GG_GCF_TABLE || opt->gcf_kind == GG_GCF_WPHASE)
     GG_CUDA(cudaMemcpyAsync(c->h_gcf.p, gcf, vb * G * G * S * S, cudaMemcpyHostToDevice, s));
   gg_job j;
   memset(&j, 0, sizeof j);

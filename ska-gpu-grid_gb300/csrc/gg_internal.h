@@ -95,6 +95,7 @@ struct GridLaunch {
   int accum;               // GG_ACC_*
   int vals_f64;
   int gauss;
+  int wphase;              // scatter: the reference's COMPUTE_GCF factor
   float sigma;             // GAUSS: uniform over the launch
   int G;                   // oversampling, uniform over the launch
   int tile;                // uv tile side, uniform over the launch

@@ -23,13 +23,14 @@ struct KParams {
   float sigma;  // GAUSS sigma, uniform within a launch
 };
 
-// GCF value of tap (a', b') of sub-kernel (sx, sy)
-template <int S, bool GAUSS, typename VT>
+// GCF value of tap (a', b') of sub-kernel (sx, sy); KIND 0 table, 1 Gaussian
+// computed on the fly, 2 the reference's per-visibility COMPUTE_GCF factor
+template <int S, int KIND, typename VT>
 struct GcfSrc;
 
 // tabulated: the reference's [G*G][S][S] layout (grid.cu:169-172)
 template <int S, typename VT>
-struct GcfSrc<S, false, VT> {
+struct GcfSrc<S, 0, VT> {
   using VT2 = typename vec2_of<VT>::type;
   const VT2 *tab;
   int G;
@@ -44,7 +45,7 @@ struct GcfSrc<S, false, VT> {
 // COMPUTE_GCF: separable Gaussian from per-CTA 1-D factors g1[s*S + a'],
 // evaluated in the prologue with expf (real, imaginary part zero)
 template <int S, typename VT>
-struct GcfSrc<S, true, VT> {
+struct GcfSrc<S, 1, VT> {
   const float *g1;
   __device__ __forceinline__ void value(int sx, int sy, int ap, int bp, VT &gr,
                                         VT &gi) const {
@@ -52,6 +53,33 @@ struct GcfSrc<S, true, VT> {
     gi = (VT)0;
   }
 };
+
+// COMPUTE_GCF as the reference's scatter kernel evaluates it: one factor per
+// visibility (set by the caller from wphase_factor), the same for every tap
+template <int S, typename VT>
+struct GcfSrc<S, 2, VT> {
+  float fr, fi;
+  __device__ __forceinline__ void value(int, int, int, int, VT &gr, VT &gi) const {
+    gr = (VT)fr;
+    gi = (VT)fi;
+  }
+};
+
+// The factor of GcfSrc<S, 2>: (T, w) = the centre-offset table entry; dx, dy
+// in double then float, the rest in float, each step rounded as written
+// (no contraction), sine and cosine from the device library.
+__device__ __forceinline__ float2 wphase_factor(double u, double v, int mx, int sx, int my,
+                                                int sy, int G, double T, double w) {
+  const float p1 = (float)(2 * 3.1415926 * w);
+  const float p2 = (float)((double)p1 * T);
+  const float dx = (float)(__dadd_rn(__dadd_rn((double)mx, -u), sx * 1.0 / G));
+  const float dy = (float)(__dadd_rn(__dadd_rn((double)my, -v), sy * 1.0 / G));
+  const float r = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+  const float ph = __fsub_rn(p1, __fmul_rn(p2, r));
+  float s, c;
+  sincosf(ph, &s, &c);
+  return make_float2(s, c);
+}
 
 // g1[s][a'] = exp(-(a' - S/2 + 1 - s/G)^2 / (2 sigma^2)) in FP32, rows of
 // `row` entries (row = 2S repeats each row once: g1[s][a' + S] = g1[s][a'])

@@ -35,9 +35,10 @@ __device__ __forceinline__ int find_job_v(const int64_t *base, int njobs,
   return lo;
 }
 
-template <int S, class ACC, bool GAUSS>
+template <int S, class ACC, int GK>
 __global__ void __launch_bounds__(kScatterThreads)
     scatter_kernel(KParams kp) {
+  constexpr bool GAUSS = GK == 1, WPHASE = GK == 2;
   using VT = typename ACC::VT;
   using VT2 = typename vec2_of<VT>::type;
   constexpr int NT = kScatterThreads, H = S / 2;
@@ -46,6 +47,9 @@ __global__ void __launch_bounds__(kScatterThreads)
   VT2 *sval = reinterpret_cast<VT2 *>(smem + NT * sizeof(int4));  // [NT][P]
   float *g1 = reinterpret_cast<float *>(smem + NT * sizeof(int4) +
                                         (size_t)NT * kp.P * sizeof(VT2));
+  // WPHASE: the per-visibility factor, beside the record
+  float2 *sfac = reinterpret_cast<float2 *>(smem + NT * sizeof(int4) +
+                                            (size_t)NT * kp.P * sizeof(VT2) + 64 * S * 4);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int P = kp.P;
   if constexpr (GAUSS) gauss_fill(g1, S, kp.G, kp.sigma, tid, NT);
@@ -94,6 +98,21 @@ __global__ void __launch_bounds__(kScatterThreads)
           r = make_int4(mx, my, sx | (sy << 8) | (tab << 16), j);
           const VT2 *v = reinterpret_cast<const VT2 *>(J.vals) + n * P;
           for (int p = 0; p < P; ++p) sval[tid * P + p] = __ldg(v + p);
+          if constexpr (WPHASE) {
+            // (T, w) at the centre offset S(S-1)/2-1 of the table
+            const VT2 tw = __ldg(reinterpret_cast<const VT2 *>(J.gcf) + (S * (S - 1) / 2 - 1));
+            double u, vv;
+            if (J.uv_f64) {
+              const double2 c = __ldg(reinterpret_cast<const double2 *>(J.uv) + n);
+              u = c.x;
+              vv = c.y;
+            } else {
+              const float2 c = __ldg(reinterpret_cast<const float2 *>(J.uv) + n);
+              u = c.x;
+              vv = c.y;
+            }
+            sfac[tid] = wphase_factor(u, vv, mx, sx, my, sy, J.G, (double)tw.x, (double)tw.y);
+          }
         }
       }
       rec[tid] = r;
@@ -106,9 +125,12 @@ __global__ void __launch_bounds__(kScatterThreads)
       const int N = J.N;
       const size_t NN = (size_t)N * N;
       const int sx = r.z & 0xff, sy = (r.z >> 8) & 0xff, tab = r.z >> 16;
-      GcfSrc<S, GAUSS, VT> gsrc;
+      GcfSrc<S, GK, VT> gsrc;
       if constexpr (GAUSS) {
         gsrc.g1 = g1;
+      } else if constexpr (WPHASE) {
+        gsrc.fr = sfac[q].x;
+        gsrc.fi = sfac[q].y;
       } else {
         gsrc.tab = reinterpret_cast<const VT2 *>(J.gcf) + (size_t)tab * J.G * J.G * S * S;
         gsrc.G = J.G;
@@ -165,12 +187,13 @@ __global__ void __launch_bounds__(kScatterThreads)
   }
 }
 
-template <int S, class ACC, bool GAUSS>
+template <int S, class ACC, int GK>
 static cudaError_t scatter_launch(const KParams &kp, int sm_count, cudaStream_t s) {
   using VT2 = typename vec2_of<typename ACC::VT>::type;
   size_t smem = kScatterThreads * sizeof(int4) +
-                (size_t)kScatterThreads * kp.P * sizeof(VT2) + 64 * S * 4;
-  auto kern = scatter_kernel<S, ACC, GAUSS>;
+                (size_t)kScatterThreads * kp.P * sizeof(VT2) + 64 * S * 4 +
+                (GK == 2 ? kScatterThreads * sizeof(float2) : 0);
+  auto kern = scatter_kernel<S, ACC, GK>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
@@ -190,14 +213,16 @@ static cudaError_t scatter_launch(const KParams &kp, int sm_count, cudaStream_t 
 template <int S>
 static cudaError_t scatter_dispatch(const GridLaunch &g, const KParams &kp,
                                     cudaStream_t s) {
-  if (g.vals_f64)
-    return g.gauss ? scatter_launch<S, AccF64, true>(kp, g.sm_count, s)
-                   : scatter_launch<S, AccF64, false>(kp, g.sm_count, s);
-  if (g.accum == GG_ACC_COMPENSATED)
-    return g.gauss ? scatter_launch<S, AccComp, true>(kp, g.sm_count, s)
-                   : scatter_launch<S, AccComp, false>(kp, g.sm_count, s);
-  return g.gauss ? scatter_launch<S, AccF32, true>(kp, g.sm_count, s)
-                 : scatter_launch<S, AccF32, false>(kp, g.sm_count, s);
+  // GCF source: 0 table, 1 Gaussian on the fly, 2 COMPUTE_GCF phase factor
+  const int gk = g.wphase ? 2 : (g.gauss ? 1 : 0);
+#define GG_SC(ACCT)                                                      \
+  return gk == 2 ? scatter_launch<S, ACCT, 2>(kp, g.sm_count, s)         \
+                 : (gk == 1 ? scatter_launch<S, ACCT, 1>(kp, g.sm_count, s) \
+                            : scatter_launch<S, ACCT, 0>(kp, g.sm_count, s))
+  if (g.vals_f64) GG_SC(AccF64);
+  if (g.accum == GG_ACC_COMPENSATED) GG_SC(AccComp);
+  GG_SC(AccF32);
+#undef GG_SC
 }
 
 cudaError_t launch_scatter(const GridLaunch &g, cudaStream_t s) {

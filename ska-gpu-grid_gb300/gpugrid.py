@@ -34,7 +34,7 @@ C64, C128 = 0, 1
 MODE_SCATTER, MODE_GATHER, MODE_WINDOW, MODE_AUTO = range(4)
 LAYOUT_INTERLEAVED, LAYOUT_PLANAR, LAYOUT_REFERENCE = range(3)
 ACC_PLAIN, ACC_COMPENSATED = range(2)
-GCF_TABLE, GCF_GAUSSIAN, GCF_COUNT = range(3)
+GCF_TABLE, GCF_GAUSSIAN, GCF_COUNT, GCF_WPHASE = range(4)
 
 MODES = {"scatter": MODE_SCATTER, "gather": MODE_GATHER,
          "window": MODE_WINDOW, "auto": MODE_AUTO}
@@ -180,7 +180,7 @@ class Options:
     mode: int = MODE_SCATTER            # Makefile GATHER= / MOVING_WINDOW=
     layout: int = LAYOUT_REFERENCE
     accum: int = ACC_PLAIN
-    gcf_kind: int = GCF_TABLE           # COMPUTE_GCF=1 -> GCF_GAUSSIAN
+    gcf_kind: int = GCF_TABLE           # COMPUTE_GCF=1 -> GCF_WPHASE (or GCF_GAUSSIAN)
     oversample: int = 8                 # GCF_GRID
     polarizations: int = 1              # POLARIZATIONS
     tile: int = 0                       # 0: chosen by method and support

@@ -386,6 +386,47 @@ def test_real_and_nearly_real_tables(ctx, imag):
     assert rel_err(got, oracle_for(uv, vals, gcf, N, S)) <= TOL["cc_comp"]
 
 
+@pytest.mark.parametrize("prec", ["cc_comp", "zz"])
+@pytest.mark.parametrize("mode", ["scatter", "window"])
+def test_compute_gcf_phase_factor(ctx, prec, mode):
+    """GG_GCF_WPHASE, the reference scatter kernel's COMPUTE_GCF factor
+    (grid_gpu.cu:103-108, 137-147), against its oracle restatement; any
+    requested method grids it by scatter.  FP32 sine/cosine of the phase on
+    the device vs libm on the host: 1e-5."""
+    S, N = 16, 256
+    uv, vals = synth.uniform(20000, 2, N - 2, seed=91,
+                             vals_dtype=np.complex128 if prec == "zz" else np.complex64)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S))
+    gcf.reshape(-1)[S * (S - 1) // 2 - 1] = 0.4 + 0.9j   # (T, w)
+    gcf = gcf.astype(np.complex128 if prec == "zz" else np.complex64)
+    o = opts_for(mode, prec, layout=gg.LAYOUT_INTERLEAVED, gcf_kind=gg.GCF_WPHASE)
+    got, flags = run(ctx, o, uv, vals, gcf, N, S, prec)
+    assert flags == [0, 0, 0, 0]
+    want = O.grid_pz_wphase(uv, to_pairs(vals), to_pairs(gcf), N, S, nthreads=8)
+    assert rel_err(got, want) <= 1e-5
+
+
+def test_compute_gcf_dropin_host_entry(ctx):
+    """The drop-in entry with COMPUTE_GCF set globally (as -D__COMPUTE_GCF
+    does through grid_gpu.cuh): padded output, reference semantics."""
+    S, N = 8, 128
+    uv, vals = synth.uniform(5000, 2, N - 2, seed=92, vals_dtype=np.complex128)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S))
+    gcf.reshape(-1)[S * (S - 1) // 2 - 1] = 1.5 + 0.25j
+    gg.set_global_options(gg.Options(gcf_kind=gg.GCF_WPHASE))
+    try:
+        out = np.zeros(gg.padded_size(N, S), np.complex128)
+        in_ = np.ascontiguousarray(uv[:, 0] + 1j * uv[:, 1])
+        gg.gridGPU(out, in_, vals, len(uv), N, np.ascontiguousarray(gcf.reshape(-1)), S)
+    finally:
+        gg.set_global_options(gg.Options())
+    h = gg.grid_head(N, S)
+    grid = out[h:h + N * N].reshape(N, N)
+    want = O.grid_pz_wphase(uv, to_pairs(vals), to_pairs(gcf), N, S)
+    got = np.stack([grid.real, grid.imag]).reshape(2, 1, N, N)
+    assert rel_err(got, want) <= 1e-5
+
+
 def test_per_visibility_gcf_rejected_by_gather(ctx):
     N, S = 64, 8
     d = [torch.zeros((10, 2), dtype=torch.float64, device="cuda"),

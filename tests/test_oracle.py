@@ -137,3 +137,27 @@ def test_oracle_per_visibility_tables():
     got = O.grid_pz_gcfinx(uv, v, idx, stack, 64, S, nthreads=4)
     want = sum(O.grid_pz(uv[idx == k], v[idx == k], tabs[k], 64, S) for k in range(3))
     assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+
+
+def test_oracle_wphase_factor_is_the_reference_formula():
+    """COMPUTE_GCF restatement: with T = 0 the factor is the constant
+    (sin 2 pi w, cos 2 pi w) in float, i.e. the plain oracle with a constant
+    table; with T != 0 it depends on the sub-pixel position only."""
+    S, G, N = 8, 8, 64
+    uv, v = synth.uniform(2000, 6, 58, seed=5)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S))
+    off = S * (S - 1) // 2 - 1
+    w = 0.123
+    gcf.reshape(-1)[off] = 0.0 + 1j * w
+    p1 = np.float32(2 * 3.1415926 * w)
+    const = np.full(G * G * S * S, complex(np.sin(p1), np.cos(p1)))
+    got = O.grid_pz_wphase(uv, v, gcf, N, S, nthreads=2)
+    want = O.grid_pz(uv, v, const, N, S)
+    assert np.abs(got - want).max() <= 1e-6 * np.abs(want).max()
+    # T != 0: two visibilities with the same sub-pixel offset get the same factor
+    gcf.reshape(-1)[off] = 3.0 + 1j * w
+    one = np.array([[20.25, 30.5]])
+    two = np.array([[20.25, 30.5], [40.25, 10.5]])
+    a = O.grid_pz_wphase(one, np.array([1.0 + 0j]), gcf, N, S)
+    b = O.grid_pz_wphase(two, np.array([1.0 + 0j, 0j]), gcf, N, S)
+    assert np.array_equal(a, b)
