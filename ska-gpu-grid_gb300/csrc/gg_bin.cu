@@ -29,6 +29,15 @@ __device__ __forceinline__ int find_job64(const int64_t *base, int njobs,
   }
   return lo;
 }
+// Job of visibility g when the warp's first visibility g0 (<= g) belongs to
+// job j0: jobs are contiguous in g, so the search is done once per warp with
+// uniform loads and each lane only steps forward past job ends.
+__device__ __forceinline__ int job_from(const int64_t *base, int njobs, int j0, int64_t g) {
+  int j = j0;
+  while (j + 1 < njobs && __ldg(base + j + 1) <= g) ++j;
+  return j;
+}
+
 __device__ __forceinline__ int find_job32(const int *base, int njobs, int g) {
   int lo = 0, hi = njobs - 1;
   while (lo < hi) {
@@ -91,8 +100,9 @@ __global__ void __launch_bounds__(256) bin_count_kernel(BinBuffers b) {
     bool valid = g < b.total_vis;
     int key = -1;
     bool bad = false;
+    const int jw = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, base);
     if (valid) {
-      int j = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, g);
+      int j = b.njobs == 1 ? 0 : job_from(b.vis_base, b.njobs, jw, g);
       const BinJob &J = b.jobs[j];
       int mx, sx, my, sy;
       int2 pk = make_int2(INT_MIN, INT_MIN);
@@ -158,8 +168,9 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(BinBuffers b) {
       start = __shfl_sync(0xffffffffu, start, leader);
       if (key >= 0) pos = start + __popc(peers & lanemask_lt());
     }
+    const int jw = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, base);
     if (pos >= 0) {
-      int j = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, g);
+      int j = b.njobs == 1 ? 0 : job_from(b.vis_base, b.njobs, jw, g);
       const BinJob &J = b.jobs[j];
       const int2 pk = b.packed[g];
       b.sorted_idx[pos] = b.window_records
