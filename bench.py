@@ -797,7 +797,7 @@ def single_options(w):
         mode=gg.MODES[w["mode"]],
         accum=gg.ACC_COMPENSATED if w["accum"] == "comp" else gg.ACC_PLAIN,
         gcf_kind=gg.GCF_GAUSSIAN if w.get("gcf") == "gauss" else gg.GCF_TABLE,
-        layout=gg.LAYOUT_INTERLEAVED)
+        layout=gg.LAYOUT_INTERLEAVED, autotune=True)
 
 
 def run_single(args, rank, world, local_rank, dist):
@@ -921,6 +921,7 @@ def run_single(args, rank, world, local_rank, dist):
         "config": {"workload": f"{args.workload}: {w['desc']}", "method": mode_name,
                    "l2": "flushed before every timed step (256 MiB write)",
                    "img_dim": N, "gcf_dim": S, "oversample": 8, "visibilities": n,
+                   "autotune": gg.autotune_report().splitlines(),
                    "parallelism": f"replicas x{world}"},
         "tap_updates_per_s": round(value * 1e6 * S * S, 1),
         "phase_ms": {"setup_and_binning": round(statistics.mean(bin_ms), 4),

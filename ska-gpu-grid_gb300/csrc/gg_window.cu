@@ -234,7 +234,7 @@ __host__ __device__ constexpr int win_min_ctas(int S, int W, int MODE) {
   return S <= 4 ? 2
          : S <= 8 ? (W == 1 ? 2 : (MODE == 2 ? 3 : 4))
          : S <= 16 ? (W == 1 ? 1 : (MODE == 2 ? 2 : 3))
-                   : 1;
+                   : (W == 8 ? 2 : 1);
 }
 
 template <int S, int W, int MODE, bool GAUSS>
