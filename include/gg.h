@@ -102,7 +102,10 @@ typedef struct gg_options {
                             The trials grid the batch itself (writing its
                             outputs, which the real launch then rewrites);
                             gg_plan_create runs them at creation, on the
-                            inputs present then.                           */
+                            inputs present then.  2 = reuse the choices
+                            made so far (the nearest size class of the same
+                            support and arithmetic; defaults when there is
+                            none) and never time trials.                   */
   int32_t reserved[5];
 } gg_options;
 
@@ -266,6 +269,7 @@ int gg_bin(gg_context *ctx, const gg_options *opt, int uv_type, const void *uv,
  * grid ready on the host side of the stream. */
 typedef struct gg_server gg_server;
 
+#define GG_SERVER_TUNE_BATCHES 32
 #define GG_REQ_INPUTS_ON_DEVICE 1 /* uv / vals are device pointers            */
 #define GG_REQ_OUT_ON_DEVICE 2    /* out is a caller-owned device grid         */
 #define GG_REQ_KEEP_RESIDENT 4    /* out unused: the grid stays on the device,
@@ -278,7 +282,12 @@ typedef struct gg_server_config {
   int32_t reserved0;
   int64_t max_batch_vis;    /* per launch (default 2^26)                    */
   int64_t hbm_budget_bytes; /* admission budget (default 150e9)             */
-  gg_options options;       /* method, accumulation, ... of every request   */
+  gg_options options;       /* method, accumulation, ... of every request;
+                               autotune 1 times trials only in the server's
+                               first GG_SERVER_TUNE_BATCHES batches, later
+                               batches run as autotune 2, so that no trial
+                               lands on the latency path of a request
+                               under load                                   */
   int64_t reserved[4];
 } gg_server_config;
 

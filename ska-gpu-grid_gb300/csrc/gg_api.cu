@@ -173,6 +173,8 @@ static int check_options(const gg_options *o) {
   if (o->group_warps != 0 && o->group_warps != 1 && o->group_warps != 2 &&
       o->group_warps != 4 && o->group_warps != 8)
     return fail(GG_ERR_ARG, "options: group_warps %d not in {0,1,2,4,8}", o->group_warps);
+  if (o->autotune < 0 || o->autotune > 2)
+    return fail(GG_ERR_ARG, "options: autotune %d not in {0,1,2}", o->autotune);
   return GG_OK;
 }
 
@@ -924,7 +926,7 @@ static int enqueue_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs
 // overwrites; they synchronise stream s.
 static int autotune_batch(gg_context *c, const gg_options *opt, const gg_job *jobs, int njobs,
                           cudaStream_t s) {
-  if (!opt->autotune || !tunable(opt) || njobs < 1 || !jobs) return GG_OK;
+  if (opt->autotune != 1 || !tunable(opt) || njobs < 1 || !jobs) return GG_OK;
   int maxS = 0;
   for (int j = 0; j < njobs; ++j) maxS = std::max<int>(maxS, (int)jobs[j].gcf_dim);
   if (resolve_mode(opt, maxS, jobs[0].vals_type == GG_C128) != GG_MODE_WINDOW) return GG_OK;

@@ -59,6 +59,7 @@ struct Slot {
   std::vector<Req *> batch;
   bool busy = false;
   bool done = false;
+  int64_t seq = 0;  // batches the server launched before this one
   struct gg_server *srv = nullptr;
 };
 
@@ -90,6 +91,7 @@ struct gg_server {
   std::vector<Feeder> feeders;
   std::mutex feeders_mu;  // guards `feeders` (client threads)
   int feeders_running = 0;
+  int64_t n_launched = 0;  // batches launched since creation (not reset)
   // statistics
   int64_t n_submitted = 0, n_completed = 0, n_failed = 0, n_rejected = 0,
           n_cancelled = 0, n_batches = 0, n_batch_jobs = 0, n_vis = 0;
@@ -233,8 +235,11 @@ void launch_batch(gg_server *srv, Slot *slot) {
     j.out_type = r.out_type;
     jobs.push_back(j);
   }
-  if (st == GG_OK) st = gg_grid_batch(slot->ctx, &srv->cfg.options, jobs.data(),
-                                      (int32_t)jobs.size(), s);
+  // autotuner trials (which synchronise the slot's stream) only while the
+  // server is young; afterwards the cached choices are reused
+  gg_options opt = srv->cfg.options;
+  if (opt.autotune == 1 && slot->seq >= GG_SERVER_TUNE_BATCHES) opt.autotune = 2;
+  if (st == GG_OK) st = gg_grid_batch(slot->ctx, &opt, jobs.data(), (int32_t)jobs.size(), s);
   for (Req *q : slot->batch) {
     if (st != GG_OK && q->status == GG_OK) q->status = st;
     const gg_request &r = q->r;
@@ -296,6 +301,7 @@ void scheduler(gg_server *srv) {
       if (!free_slot->batch.empty()) {
         free_slot->busy = true;
         free_slot->done = false;
+        free_slot->seq = srv->n_launched++;
         ++srv->n_batches;
         srv->n_batch_jobs += (int64_t)free_slot->batch.size();
         lk.unlock();

@@ -71,6 +71,8 @@ class gg_job(ctypes.Structure):
 
 
 REQ_INPUTS_ON_DEVICE, REQ_OUT_ON_DEVICE, REQ_KEEP_RESIDENT = 1, 2, 4
+# the server times autotuner trials only during its first batches
+SERVER_TUNE_BATCHES = 32
 
 
 class gg_server_config(ctypes.Structure):
@@ -188,7 +190,8 @@ class Options:
     gcf_sigma: float = 0.0
     window_chunk: int = 0
     group_warps: int = 0                # moving window: warps per sub-grid
-    autotune: bool = False              # moving window: tile / warps / chunk by timing
+    autotune: int = 0                   # moving window: tile / warps / chunk by timing
+                                        # (1: time new size classes, 2: reuse choices)
 
     def c(self) -> gg_options:
         o = gg_options()
@@ -199,7 +202,7 @@ class Options:
         o.input_sorted = int(bool(self.input_sorted))
         o.gcf_sigma, o.window_chunk = self.gcf_sigma, self.window_chunk
         o.group_warps = self.group_warps
-        o.autotune = int(bool(self.autotune))
+        o.autotune = int(self.autotune)
         return o
 
 

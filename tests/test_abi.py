@@ -120,7 +120,8 @@ def test_abi_version_and_defaults():
 @pytest.mark.parametrize("field,value", [
     ("mode", 9), ("layout", 7), ("accum", 5), ("gcf_kind", 4),
     ("oversample", 6), ("oversample", 128), ("polarizations", 0),
-    ("polarizations", 9), ("tile", 24), ("tile", 8), ("window_chunk", -1)])
+    ("polarizations", 9), ("tile", 24), ("tile", 8), ("window_chunk", -1),
+    ("autotune", 3), ("autotune", -1)])
 def test_bad_options_rejected_with_message(field, value):
     o = gg.Options()
     c = o.c()
@@ -186,3 +187,11 @@ def test_gcf_table_matches_oracle_layout():
     import oracle as O
     g1 = synth.gaussian_gcf_1d(8)
     assert np.array_equal(synth.gcf_table(g1), O.gcf_from_1d(g1))
+
+
+def test_header_constants_match_python_mirror():
+    src = open(os.path.join(ROOT, "include", "gg.h")).read()
+    consts = dict(re.findall(r"#define (GG_\w+) (-?\d+)", src))
+    assert int(consts["GG_SERVER_TUNE_BATCHES"]) == gg.SERVER_TUNE_BATCHES
+    assert int(consts["GG_REQ_KEEP_RESIDENT"]) == gg.REQ_KEEP_RESIDENT
+    assert int(consts["GG_GCF_WPHASE"]) == gg.GCF_WPHASE

@@ -191,3 +191,48 @@ def test_server_trace_cancel_timeout(ctx):
         assert st["completed"] == len(reqs) - 1 and st["cancelled"] == 1
     for (N, S, uv, vals), (_, _, out) in zip(data[:-1], keep[:-1]):
         assert relerr(out, grid_alone(ctx, OPTS, N, S, uv, vals, GCF[S])) <= TOL
+
+
+def test_server_times_autotune_trials_only_while_young(ctx):
+    """With autotune 1 the server times trials only during its first
+    GG_SERVER_TUNE_BATCHES batches: a support class first seen later takes
+    the cached or default configuration (autotune 2) and is not timed, so no
+    trial lands on a request's latency under load.  Results stay correct."""
+    rng = np.random.default_rng(5)
+    gg.autotune_clear()
+    o = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
+                   layout=gg.LAYOUT_INTERLEAVED, autotune=1)
+    with gg.Server(streams=1, options=o) as srv:
+        gids = {S: srv.add_gcf(GCF[S]) for S in (8, 16)}
+
+        def one(S, seed):
+            N = 256
+            uv, vals = synth.tracks(N, nant=16, ntime=40, npts=4000, seed=seed)
+            out = np.full(N * N, np.nan, np.complex64)
+            t = srv.submit(gg.Server.request(uv.ctypes.data, vals.ctypes.data, out.ctypes.data,
+                                             len(uv), N, S, gids[S]))
+            assert srv.wait(t, timeout=60).status == 0
+            srv.release(t)
+            assert relerr(out, grid_alone(ctx, OPTS, N, S, uv, vals, GCF[S])) <= TOL
+
+        one(8, 500)                    # first batch: support 8 is tuned
+        assert "support 8 " in gg.autotune_report()
+        for k in range(gg.SERVER_TUNE_BATCHES):
+            one(8, 501 + k)            # one request per batch
+        assert srv.stats()["batches"] > gg.SERVER_TUNE_BATCHES
+        one(16, 600)                   # after the window: not timed
+        assert "support 16 " not in gg.autotune_report()
+    gg.autotune_clear()
+
+
+def test_autotune_lookup_only_never_times(ctx):
+    """autotune 2 reuses the cache and, with nothing cached, runs the
+    default configuration without trials."""
+    gg.autotune_clear()
+    o = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
+                   layout=gg.LAYOUT_INTERLEAVED, autotune=2)
+    N, S = 512, 16
+    uv, vals = synth.tracks(N, nant=24, ntime=400, npts=None, seed=77)
+    got = grid_alone(ctx, o, N, S, uv, vals, GCF[S])
+    assert gg.autotune_report().strip() == ""
+    assert relerr(got, grid_alone(ctx, OPTS, N, S, uv, vals, GCF[S])) <= TOL
