@@ -150,6 +150,22 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(BinBuffers b) {
     int64_t g = base + lane;
     bool valid = g < b.total_vis;
     int key = valid ? b.key[g] : -1;
+    // What is copied does not depend on the sorted position: its loads (the
+    // packed indices and the first value plane) are issued before the
+    // position's atomic, so that their latency overlaps it.
+    const int jw = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, base);
+    const BinJob *J = nullptr;
+    int64_t n = 0;
+    int2 pk = make_int2(0, 0);
+    float2 v8 = make_float2(0.f, 0.f);
+    double2 v16 = make_double2(0.0, 0.0);
+    if (key >= 0) {
+      J = b.jobs + (b.njobs == 1 ? 0 : job_from(b.vis_base, b.njobs, jw, g));
+      n = g - J->vis_base;
+      pk = b.packed[g];
+      if (b.vals_bytes == 8) v8 = __ldg((const float2 *)J->vals + n * b.P);
+      else v16 = __ldg((const double2 *)J->vals + n * b.P);
+    }
     int pos = -1;
     if (b.input_sorted) {
       if (key >= 0) {
@@ -168,24 +184,21 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(BinBuffers b) {
       start = __shfl_sync(0xffffffffu, start, leader);
       if (key >= 0) pos = start + __popc(peers & lanemask_lt());
     }
-    const int jw = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, base);
     if (pos >= 0) {
-      int j = b.njobs == 1 ? 0 : job_from(b.vis_base, b.njobs, jw, g);
-      const BinJob &J = b.jobs[j];
-      const int2 pk = b.packed[g];
       b.sorted_idx[pos] = b.window_records
-                              ? window_record(pk.x >> J.log2G, pk.x & (J.G - 1),
-                                              pk.y >> J.log2G, pk.y & (J.G - 1), J.G)
+                              ? window_record(pk.x >> J->log2G, pk.x & (J->G - 1),
+                                              pk.y >> J->log2G, pk.y & (J->G - 1), J->G)
                               : pk;
-      int64_t n = g - J.vis_base;
       if (b.vals_bytes == 8) {
-        const float2 *v = (const float2 *)J.vals + n * b.P;
+        const float2 *v = (const float2 *)J->vals + n * b.P;
         float2 *o = (float2 *)b.sorted_vals;
-        for (int p = 0; p < b.P; ++p) o[p * b.vstride + pos] = __ldg(v + p);
+        o[pos] = v8;
+        for (int p = 1; p < b.P; ++p) o[p * b.vstride + pos] = __ldg(v + p);
       } else {
-        const double2 *v = (const double2 *)J.vals + n * b.P;
+        const double2 *v = (const double2 *)J->vals + n * b.P;
         double2 *o = (double2 *)b.sorted_vals;
-        for (int p = 0; p < b.P; ++p) o[p * b.vstride + pos] = __ldg(v + p);
+        o[pos] = v16;
+        for (int p = 1; p < b.P; ++p) o[p * b.vstride + pos] = __ldg(v + p);
       }
       if (b.order) b.order[pos] = (int)g;
     }
