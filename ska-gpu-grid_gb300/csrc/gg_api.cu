@@ -835,6 +835,7 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
     b.kept_pos = pl.input_sorted ? (int *)(ws + pl.o_kept) : nullptr;
     b.window_records = pl.mode == GG_MODE_WINDOW;
     GG_CUDA(run_binning(b, s));
+    g.holes = b.bookmarks + pl.total_tiles + 1;
   }
 
   if (pl.mode == GG_MODE_WINDOW) {

@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(BinBuffers b) {
         pos = b.kept_pos[g];
         if (pos < b.bookmarks[key] || pos >= b.bookmarks[key + 1]) {
           atomicOr(&b.flags[FLAG_UNSORTED], 1);
+          b.bookmarks[b.total_tiles + 1] = 1;  // this call's records have holes
           pos = -1;
         }
       }
@@ -316,7 +317,7 @@ cudaError_t launch_vis2ints(int uv_f64, const void *uv, int64_t npts, int G,
 
 cudaError_t run_binning(const BinBuffers &b, cudaStream_t s) {
   cudaError_t e;
-  e = cudaMemsetAsync(b.bookmarks, 0, sizeof(int) * (size_t)(b.total_tiles + 1), s);
+  e = cudaMemsetAsync(b.bookmarks, 0, sizeof(int) * (size_t)(b.total_tiles + 2), s);
   if (e != cudaSuccess) return e;
   if (b.total_vis > 0) {
     bin_count_kernel<<<grid_for(b.total_vis), 256, 0, s>>>(b);

@@ -42,6 +42,9 @@ __global__ void __launch_bounds__(kGatherThreads)
   using VT2 = typename vec2_of<VT>::type;
   using Sh = GatherShape<VT2>;
   constexpr int K = kGatherChunk, H = S / 2, TT = kGatherTile;
+  // unsorted input declared sorted: holes in this call's sorted records, the
+  // call fails with GG_ERR_UNSORTED -- grid nothing
+  if (kp.holes && *kp.holes) return;
   extern __shared__ __align__(16) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
   // double buffers, addressed arithmetically (buffer b at +b*size)
@@ -242,6 +245,7 @@ cudaError_t launch_gather(const GridLaunch &g, cudaStream_t s) {
   KParams kp{};
   kp.jobs = g.jobs;
   kp.flags = g.flags;
+  kp.holes = g.holes;
   kp.njobs = g.njobs;
   kp.tile_base = g.tile_base;
   kp.total_tiles = g.total_tiles;

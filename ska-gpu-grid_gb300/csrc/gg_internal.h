@@ -39,7 +39,9 @@ struct BinBuffers {
   int P;                   // polarisations (uniform over the batch)
   int2 *packed;            // [total_vis]
   int *key;                // [total_vis] global tile id or -1 (dropped)
-  int *bookmarks;          // [total_tiles+1]: counts, then exclusive offsets
+  int *bookmarks;          // [total_tiles+1]: counts, then exclusive offsets;
+                           // [total_tiles+1]: set when input declared sorted
+                           // is not (records left unwritten)
   int *cursor;             // [total_tiles]
   int *scan_tmp;           // scratch for the multi-level scan
   int2 *sorted_idx;        // [total_vis + pad]
@@ -102,6 +104,7 @@ struct GridLaunch {
   int group_warps;         // moving window: warps per sub-grid (0: by support)
   int P;
   int *flags;
+  const int *holes;        // binned methods: bookmarks[total_tiles + 1]
   int sm_count;
   // scatter: global visibility space
   const int64_t *vis_base; // device [njobs+1]

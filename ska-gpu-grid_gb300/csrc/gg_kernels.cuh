@@ -12,6 +12,9 @@ struct KParams {
   const int *nitems;
   int *item_next;
   int *flags;
+  // nonzero when this call's binning found input declared tile-sorted to be
+  // unsorted (its sorted records then have holes); null without binning
+  const int *holes;
   const int64_t *vis_base;
   const int *tile_base;
   int64_t total_vis;

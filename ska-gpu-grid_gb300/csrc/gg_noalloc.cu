@@ -252,6 +252,7 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   g.tile = T;
   g.P = 1;
   g.flags = flags;
+  g.holes = b.bookmarks + b.total_tiles + 1;
   g.sm_count = sms;
   g.items = items;
   g.nitems = flags + 8;

@@ -96,6 +96,9 @@ template <> struct WinAcc<0> {
   using VT = float;
   using CellT = float2;
   u64 s;
+  __device__ __forceinline__ CellT merged(const CellT o) const {
+    return upk2(add2(pk2(o.x, o.y), s));
+  }
   __device__ __forceinline__ void zero() { s = 0ull; }
   __device__ __forceinline__ void add(u64 t) { s = add2(s, t); }
   __device__ __forceinline__ void fma(u64 v, u64 g) { s = fma2(v, g, s); }
@@ -115,6 +118,12 @@ template <> struct WinAcc<1> {
   using VT = float;
   using CellT = float4;
   u64 s;
+  __device__ __forceinline__ CellT merged(const CellT o) const {
+    u64 e;
+    const u64 h = two_sum2(pk2(o.x, o.y), s, e);
+    const float2 hf = upk2(h), lf = upk2(add2(pk2(o.z, o.w), e));
+    return make_float4(hf.x, hf.y, lf.x, lf.y);
+  }
   __device__ __forceinline__ void zero() { s = 0ull; }
   __device__ __forceinline__ void add(u64 t) { s = add2(s, t); }
   __device__ __forceinline__ void fma(u64 v, u64 g) { s = fma2(v, g, s); }
@@ -134,6 +143,9 @@ template <> struct WinAcc<2> {
   using VT = double;
   using CellT = double2;
   double re, im;
+  __device__ __forceinline__ CellT merged(const CellT o) const {
+    return make_double2(__dadd_rn(o.x, re), __dadd_rn(o.y, im));
+  }
   __device__ __forceinline__ void zero() { re = im = 0.0; }
   // adds v * g for packed FP32 pairs (v complex, g = (r, r) real factor)
   __device__ __forceinline__ void fma(u64 v, u64 g) {
@@ -247,6 +259,10 @@ __global__ void __launch_bounds__(kWinThreads, win_min_ctas(S, W, MODE))
   using CellT = typename L::CellT;
   constexpr int NGT = Cfg::NGT, Q = Cfg::Q, K = Cfg::K, GROUPS = Cfg::GROUPS;
   constexpr int H = S / 2;
+  // Input declared tile-sorted but found unsorted by this call's binning:
+  // the sorted records have holes (never written) and the call fails with
+  // GG_ERR_UNSORTED -- grid nothing.
+  if (kp.holes && *kp.holes) return;
 
   extern __shared__ __align__(16) unsigned char smem[];
   float *g1 = reinterpret_cast<float *>(smem);
@@ -494,14 +510,40 @@ __global__ void __launch_bounds__(kWinThreads, win_min_ctas(S, W, MODE))
             const int b0 = (ry[0] - fy0) & (S - 1);
             pofs = GAUSS ? b0 : b0 * S + pax;
             const int lx = fx0 + pax - ox;
+            if constexpr (S * S % NGT == 0) {
+              // Every register sum goes to its cell on a footprint move,
+              // changed or not: the Q read-modify-writes of a thread are
+              // issued together (distinct cells, no aliasing) instead of one
+              // branch per residue, which a warp takes whenever any lane's
+              // cell changed -- on most moves.  Adding a sum into a cell that
+              // stays current only splits a register run.  A sum with no
+              // cell yet is zero and goes to its new cell.
+              int cc[Q], lcs[Q];
+              CellT cv[Q];
 #pragma unroll
-            for (int k = 0; k < Q; ++k) {
-              const int bp = (b0 + k * D) & (S - 1);
-              const int lc = (S * S % NGT == 0 || rv[k]) ? (fy0 + bp - oy) * R + lx : -1;
-              if (lc != cur[k]) {
-                if (cur[k] >= 0) acc[k].into(region + cur[k]);
-                cur[k] = lc;
+              for (int k = 0; k < Q; ++k) {
+                const int bp = (b0 + k * D) & (S - 1);
+                lcs[k] = (fy0 + bp - oy) * R + lx;
+                cc[k] = cur[k] >= 0 ? cur[k] : lcs[k];
+                cv[k] = region[cc[k]];
+              }
+#pragma unroll
+              for (int k = 0; k < Q; ++k) region[cc[k]] = acc[k].merged(cv[k]);
+#pragma unroll
+              for (int k = 0; k < Q; ++k) {
+                cur[k] = lcs[k];
                 acc[k].zero();
+              }
+            } else {
+#pragma unroll
+              for (int k = 0; k < Q; ++k) {
+                const int bp = (b0 + k * D) & (S - 1);
+                const int lc = (S * S % NGT == 0 || rv[k]) ? (fy0 + bp - oy) * R + lx : -1;
+                if (lc != cur[k]) {
+                  if (cur[k] >= 0) acc[k].into(region + cur[k]);
+                  cur[k] = lc;
+                  acc[k].zero();
+                }
               }
             }
           }
@@ -776,6 +818,7 @@ cudaError_t launch_window(const GridLaunch &g, cudaStream_t s) {
   kp.nitems = g.nitems;
   kp.item_next = g.item_next;
   kp.flags = g.flags;
+  kp.holes = g.holes;
   kp.njobs = g.njobs;
   kp.P = g.P;
   kp.T = g.tile;
