@@ -28,8 +28,9 @@
 //    item is claimed early and its first chunk prefetched while the current
 //    one is gridded).
 //  * Records come in runs with an unchanged footprint origin.  The first
-//    record of a run works out the target cells and flushes the register
-//    sums whose cell changed; the rest of the run goes through a fast loop
+//    record of a run works out the target cells and adds every register sum
+//    into its cell (the Q read-modify-writes of a thread issued together);
+//    the rest of the run goes through a fast loop
 //    that only loads GCF values (two records ahead of their use, at fixed
 //    strides in a row-doubled copy of the table) and accumulates.  Tables
 //    without imaginary parts (flagged on the device) take a real-factor
