@@ -47,6 +47,25 @@ __device__ __forceinline__ int find_job32(const int *base, int njobs, int g) {
   return lo;
 }
 
+// Contiguous slice [w0, w1) of the visibilities for this warp (multiples of
+// 32 apart), walked 32 at a time: the job of the slice's first visibility is
+// found once and then only advanced, where a grid-stride walk would search
+// the job table (dependent loads) on every step.
+struct WarpSlice {
+  int64_t w0, w1;
+  __device__ WarpSlice(int64_t total) {
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t per = ((total + nwarps - 1) / nwarps + 31) & ~(int64_t)31;
+    w0 = min(total, wid * per);
+    w1 = min(total, w0 + per);
+  }
+};
+__device__ __forceinline__ int advance_job(const int64_t *base, int njobs, int j, int64_t g) {
+  while (j + 1 < njobs && __ldg(base + j + 1) <= g) ++j;
+  return j;
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -94,13 +113,14 @@ __global__ void __launch_bounds__(256)
 //    their on-grid taps still lie inside that tile's window region
 __global__ void __launch_bounds__(256) bin_count_kernel(BinBuffers b) {
   const int lane = threadIdx.x & 31;
-  for (int64_t base = blockIdx.x * 256ll + (threadIdx.x & ~31);
-       base < b.total_vis; base += (int64_t)gridDim.x * 256) {
+  const WarpSlice ws(b.total_vis);
+  int jw = b.njobs == 1 || ws.w0 >= ws.w1 ? 0 : find_job64(b.vis_base, b.njobs, ws.w0);
+  for (int64_t base = ws.w0; base < ws.w1; base += 32) {
     int64_t g = base + lane;
-    bool valid = g < b.total_vis;
+    bool valid = g < ws.w1;
     int key = -1;
     bool bad = false;
-    const int jw = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, base);
+    if (b.njobs > 1) jw = advance_job(b.vis_base, b.njobs, jw, base);
     if (valid) {
       int j = b.njobs == 1 ? 0 : job_from(b.vis_base, b.njobs, jw, g);
       const BinJob &J = b.jobs[j];
@@ -145,15 +165,16 @@ __global__ void __launch_bounds__(256) bin_count_kernel(BinBuffers b) {
 //                  tile's range proves the input was not tile-sorted
 __global__ void __launch_bounds__(256) bin_scatter_kernel(BinBuffers b) {
   const int lane = threadIdx.x & 31;
-  for (int64_t base = blockIdx.x * 256ll + (threadIdx.x & ~31);
-       base < b.total_vis; base += (int64_t)gridDim.x * 256) {
+  const WarpSlice ws(b.total_vis);
+  int jw = b.njobs == 1 || ws.w0 >= ws.w1 ? 0 : find_job64(b.vis_base, b.njobs, ws.w0);
+  for (int64_t base = ws.w0; base < ws.w1; base += 32) {
     int64_t g = base + lane;
-    bool valid = g < b.total_vis;
+    bool valid = g < ws.w1;
     int key = valid ? b.key[g] : -1;
     // What is copied does not depend on the sorted position: its loads (the
     // packed indices and the first value plane) are issued before the
     // position's atomic, so that their latency overlaps it.
-    const int jw = b.njobs == 1 ? 0 : find_job64(b.vis_base, b.njobs, base);
+    if (b.njobs > 1) jw = advance_job(b.vis_base, b.njobs, jw, base);
     const BinJob *J = nullptr;
     int64_t n = 0;
     int2 pk = make_int2(0, 0);

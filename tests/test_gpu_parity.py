@@ -165,6 +165,30 @@ def test_unsorted_input_detected(ctx):
     assert e.value.code == gg.ERR_UNSORTED
 
 
+@pytest.mark.parametrize("mode", ["window", "gather"])
+def test_unsorted_flag_does_not_block_later_calls(ctx, mode):
+    """Device entry point: a call whose declared-sorted input is unsorted
+    raises the (sticky) unsorted flag and grids nothing; the next call on the
+    same context, made before the flags are read, still grids in full."""
+    N, S = 256, 8
+    uv, vals = synth.uniform(5000, 8, N - 8, seed=11)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    d_uv, d_v = torch.from_numpy(uv).cuda(), torch.from_numpy(vals).cuda()
+    d_g = torch.from_numpy(gcf.reshape(-1)).cuda()
+    out = torch.full((N * N,), float("nan"), dtype=torch.complex64, device="cuda")
+    layout = gg.LAYOUT_INTERLEAVED
+    ctx.grid(gg.Options(mode=MODES[mode], input_sorted=True, layout=layout),
+             out, d_uv, d_v, d_g, N, S)
+    ctx.grid(gg.Options(mode=MODES[mode], accum=gg.ACC_COMPENSATED, layout=layout),
+             out, d_uv, d_v, d_g, N, S)
+    torch.cuda.synchronize()
+    flags = ctx.read_flags()
+    assert flags[2] == 1 and flags[1] == 0  # unsorted seen, no wait timed out
+    host = torch.view_as_real(out).reshape(-1).cpu().numpy()
+    ref = oracle_for(uv, vals, gcf, N, S)
+    assert rel_err(planar_from_grid(host, 1, N, False), ref) <= TOL["cc_comp"]
+
+
 def test_out_of_table_index_dropped_and_counted(ctx):
     """u right below an integer is not float-representable: the CPU gridder's
     oversample index becomes -1 (outside its table); the GPU path drops the
