@@ -343,7 +343,7 @@ def cudart():
 
 
 # ---------------------------------------------------------------------------
-# served stream (config 5) -- the headline
+# served stream of 10,000 requests -- the headline
 # ---------------------------------------------------------------------------
 def run_served(args, rank, world, local_rank, dist):
     import torch
@@ -607,7 +607,7 @@ def run_served(args, rank, world, local_rank, dist):
 
 
 # ---------------------------------------------------------------------------
-# batched plan in a CUDA graph (config 4)
+# batched plan of 256 jobs in a CUDA graph
 # ---------------------------------------------------------------------------
 def run_batch(args, rank, world, local_rank, dist):
     import torch
@@ -781,7 +781,7 @@ def run_batch(args, rank, world, local_rank, dist):
 
 
 # ---------------------------------------------------------------------------
-# single job (configs 1-3)
+# single job (uniform1024, tracks4096, disk8192)
 # ---------------------------------------------------------------------------
 def make_single(w, seed):
     import synth

@@ -157,7 +157,7 @@ def set_bookmarks(packed, blocksize: int, blockgrid: int,
 
 def gaussian_gcf(gcf_dim: int, sigma: float | None = None, gcf_grid: int = 8):
     """(table complex128 [G*G, S, S], g1 float64 [G, S]); sigma defaults to
-    S/4, the configs' separable Gaussian."""
+    S/4, the separable Gaussian of the benchmark workloads."""
     if sigma is None:
         sigma = gcf_dim / 4.0
     tab = np.empty((gcf_grid * gcf_grid, gcf_dim, gcf_dim, 2), np.float64)
