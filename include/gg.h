@@ -85,7 +85,8 @@ typedef struct gg_options {
   int32_t gcf_kind;      /* GG_GCF_*                                         */
   int32_t oversample;    /* GCF_GRID: power of two, 1..64 (default 8)        */
   int32_t polarizations; /* POLARIZATIONS: 1..8 (default 1)                  */
-  int32_t tile;          /* uv tile side in cells for binning; 0 = chosen by
+  int32_t tile;          /* uv tile side in cells for binning, a power of
+                            two in 8..256 (gather: 32); 0 = chosen by
                             method and support (default)                  */
   int32_t input_sorted;  /* 1: caller guarantees visibilities are grouped by
                             uv tile (of `tile` cells, 32 when tile is 0) in

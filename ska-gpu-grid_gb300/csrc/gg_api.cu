@@ -166,8 +166,8 @@ static int check_options(const gg_options *o) {
   if (o->polarizations < 1 || o->polarizations > kMaxPols)
     return fail(GG_ERR_ARG, "options: polarizations %d outside 1..%d",
                 o->polarizations, kMaxPols);
-  if (o->tile != 0 && (!is_pow2(o->tile) || o->tile < 16 || o->tile > 256))
-    return fail(GG_ERR_ARG, "options: tile %d must be 0 or a power of two in 16..256",
+  if (o->tile != 0 && (!is_pow2(o->tile) || o->tile < 8 || o->tile > 256))
+    return fail(GG_ERR_ARG, "options: tile %d must be 0 or a power of two in 8..256",
                 o->tile);
   if (o->window_chunk < 0) return fail(GG_ERR_ARG, "options: window_chunk < 0");
   if (o->group_warps != 0 && o->group_warps != 1 && o->group_warps != 2 &&
@@ -921,10 +921,10 @@ static int enqueue_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs
 
 // Autotuner.  For every support class of a moving-window batch whose size
 // class has no entry yet, time candidate configurations on the class's own
-// jobs (coordinate descent: warps per sub-grid group, then tile, then records
-// per work item; two launches each, the faster counted) and record the
-// fastest.  The trials write the jobs' outputs, which the real launch then
-// overwrites; they synchronise stream s.
+// jobs (every pair of warps per sub-grid group and tile, then records per
+// work item at the best pair; two launches each, the faster counted) and
+// record the fastest.  The trials write the jobs' outputs, which the real
+// launch then overwrites; they synchronise stream s.
 static int autotune_batch(gg_context *c, const gg_options *opt, const gg_job *jobs, int njobs,
                           cudaStream_t s) {
   if (opt->autotune != 1 || !tunable(opt) || njobs < 1 || !jobs) return GG_OK;
@@ -990,21 +990,24 @@ static int autotune_batch(gg_context *c, const gg_options *opt, const gg_job *jo
         best = cf;
       }
     };
+    // warps per group and tile jointly (their best pair is not found one
+    // coordinate at a time: one-warp groups win on 8-cell tiles and lose on
+    // 16-cell ones); 8-cell tiles give smaller sub-grids and so more resident
+    // groups, not tried for support 32
     static const int kWarps[] = {1, 2, 4, 8};
+    const ClassCfg base_best = best;
     for (int w : kWarps) {
       if ((S == 4 && w != 1) || (S == 8 && w > 2) || (S == 16 && w > 4) || (S == 32 && w < 4))
         continue;
-      ClassCfg cf = best;
-      cf.W = w;
-      consider(cf);
-    }
-    if (!opt->input_sorted)
-      for (int T : {16, 32}) {
-        if (T == best.T) continue;
-        ClassCfg cf = best;
+      for (int T : {8, 16, 32}) {
+        if (opt->input_sorted && T != base_best.T) continue;
+        if (T == 8 && S > 16) continue;
+        ClassCfg cf = base_best;
+        cf.W = w;
         cf.T = T;
         consider(cf);
       }
+    }
     for (int ch : {1024, 4096}) {
       ClassCfg cf = best;
       cf.chunk = ch;

@@ -241,11 +241,12 @@ __device__ __forceinline__ void group_sync(int gid, int nthreads) {
 }
 
 // Resident CTAs per SM the register allocation is held to: as many as the
-// shared memory of the configuration allows at the default tile (16), where
-// the compiler then fits the loop without spilling; FP64 sums get one fewer.
+// shared memory of the configuration allows at the default tile (16) -- for
+// one-warp groups of support 8, at the 8-cell tile -- where the compiler then
+// fits the loop without spilling; FP64 sums get one fewer.
 __host__ __device__ constexpr int win_min_ctas(int S, int W, int MODE) {
   return S <= 4 ? 2
-         : S <= 8 ? (W == 1 ? 2 : (MODE == 2 ? 3 : 4))
+         : S <= 8 ? (W == 1 ? (MODE == 2 ? 2 : 3) : (MODE == 2 ? 3 : 4))
          : S <= 16 ? (W == 1 ? 1 : (MODE == 2 ? 2 : 3))
                    : (W == 8 ? 2 : 1);
 }

@@ -120,7 +120,7 @@ def test_abi_version_and_defaults():
 @pytest.mark.parametrize("field,value", [
     ("mode", 9), ("layout", 7), ("accum", 5), ("gcf_kind", 4),
     ("oversample", 6), ("oversample", 128), ("polarizations", 0),
-    ("polarizations", 9), ("tile", 24), ("tile", 8), ("window_chunk", -1),
+    ("polarizations", 9), ("tile", 24), ("tile", 4), ("window_chunk", -1),
     ("autotune", 3), ("autotune", -1)])
 def test_bad_options_rejected_with_message(field, value):
     o = gg.Options()

@@ -130,9 +130,10 @@ def test_vis2ints_bit_exact_fp32(ctx):
     assert np.array_equal(got, O.vis2ints(uv32.astype(np.float64)))
 
 
+@pytest.mark.parametrize("T", [8, 32])
 @pytest.mark.parametrize("input_sorted", [False, True])
-def test_bin_bookmarks(ctx, input_sorted):
-    N, S, T = 512, 8, 32
+def test_bin_bookmarks(ctx, input_sorted, T):
+    N, S = 512, 8
     uv, _ = synth.uniform(30000, 0, N, seed=9)
     if input_sorted:
         uv = uv[synth.tile_sort(uv, N, T)]
@@ -575,3 +576,16 @@ def test_linearity_and_checksum_large(ctx, mode):
     expect = (v1.astype(np.complex128) * tapsum[sy * 8 + sx]).sum()
     bound = (np.abs(v1) * np.abs(tapsum[sy * 8 + sx])).sum()
     assert abs(a.sum() - expect) <= 1e-6 * bound
+
+
+@pytest.mark.parametrize("S,W", [(4, 0), (8, 1), (8, 2), (16, 2), (16, 4), (32, 4)])
+def test_window_8_cell_tiles(ctx, S, W):
+    """The moving window on 8-cell uv tiles (more, smaller sub-grids): a
+    ragged grid with visibilities past every edge, against the oracle."""
+    N = 100
+    uv, vals = synth.uniform(6000, -S, N + S, seed=40 + S + W)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    o = opts_for("window", "cc_comp", tile=8, group_warps=W)
+    out, flags = run(ctx, o, uv, vals, gcf, N, S, "cc_comp")
+    assert flags == [0, 0, 0, 0]
+    assert rel_err(out, oracle_for(uv, vals, gcf, N, S)) <= TOL["cc_comp"]
