@@ -242,13 +242,16 @@ __device__ __forceinline__ void group_sync(int gid, int nthreads) {
 
 // Resident CTAs per SM the register allocation is held to: as many as the
 // shared memory of the configuration allows at the default tile (16) -- for
-// one-warp groups of support 8, at the 8-cell tile -- where the compiler then
-// fits the loop without spilling; FP64 sums get one fewer.
+// one-warp groups of supports 8 and 16, at the 8-cell tile -- where the
+// compiler then fits the loop (one-warp support-16 groups with a few spilled
+// bytes, measured faster than one CTA per SM); FP64 sums get one fewer.
+// Support 32 with four-warp groups: two CTAs only for plain FP32 sums, whose
+// float2 cells let two CTAs' sub-grids fit an SM.
 __host__ __device__ constexpr int win_min_ctas(int S, int W, int MODE) {
   return S <= 4 ? 2
          : S <= 8 ? (W == 1 ? (MODE == 2 ? 2 : 3) : (MODE == 2 ? 3 : 4))
-         : S <= 16 ? (W == 1 ? 1 : (MODE == 2 ? 2 : 3))
-                   : (W == 8 ? 2 : 1);
+         : S <= 16 ? (W == 1 ? (MODE == 2 ? 1 : 2) : (MODE == 2 ? 2 : 3))
+                   : (W == 8 || MODE == 0 ? 2 : 1);
 }
 
 template <int S, int W, int MODE, bool GAUSS>

@@ -578,7 +578,7 @@ def test_linearity_and_checksum_large(ctx, mode):
     assert abs(a.sum() - expect) <= 1e-6 * bound
 
 
-@pytest.mark.parametrize("S,W", [(4, 0), (8, 1), (8, 2), (16, 2), (16, 4), (32, 4)])
+@pytest.mark.parametrize("S,W", [(4, 0), (8, 1), (8, 2), (16, 1), (16, 2), (16, 4), (32, 4)])
 def test_window_8_cell_tiles(ctx, S, W):
     """The moving window on 8-cell uv tiles (more, smaller sub-grids): a
     ragged grid with visibilities past every edge, against the oracle."""
@@ -589,3 +589,17 @@ def test_window_8_cell_tiles(ctx, S, W):
     out, flags = run(ctx, o, uv, vals, gcf, N, S, "cc_comp")
     assert flags == [0, 0, 0, 0]
     assert rel_err(out, oracle_for(uv, vals, gcf, N, S)) <= TOL["cc_comp"]
+
+
+@pytest.mark.parametrize("T", [16, 32])
+@pytest.mark.parametrize("prec", ["cc", "cc_comp"])
+def test_window_support_32_four_warp_groups(ctx, prec, T):
+    """Support 32 with four-warp groups (eight residue rows per thread), plain
+    and compensated FP32 sums, ragged grid, against the oracle."""
+    N, S = 200, 32
+    uv, vals = synth.uniform(4000, -S, N + S, seed=60 + T)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+    o = opts_for("window", prec, tile=T, group_warps=4)
+    out, flags = run(ctx, o, uv, vals, gcf, N, S, prec)
+    assert flags == [0, 0, 0, 0]
+    assert rel_err(out, oracle_for(uv, vals, gcf, N, S)) <= TOL[prec]
