@@ -419,11 +419,13 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
       const int S = (int)jobs[j].gcf_dim;
       if (cfgs.count(S)) continue;
       // automatic tile: the moving window keeps one (T+S-1)^2 sub-grid per
-      // warp group, so supports up to 16 use 16-cell tiles; gather needs 32;
-      // input declared tile-sorted: the caller's tiles are the default 32
+      // warp group, so supports up to 16 use 8-cell tiles (small sub-grids,
+      // many resident groups: measured fastest on every track workload);
+      // gather needs 32; input declared tile-sorted: the caller's tiles are
+      // the default 32
       ClassCfg cf;
       cf.T = opt->tile > 0 ? opt->tile
-                           : (m0 == GG_MODE_WINDOW && S <= 16 && !opt->input_sorted ? 16 : 32);
+                           : (m0 == GG_MODE_WINDOW && S <= 16 && !opt->input_sorted ? 8 : 32);
       cf.W = opt->group_warps;
       cf.chunk = opt->window_chunk > 0 ? opt->window_chunk : 2048;
       if (m0 == GG_MODE_WINDOW && tunable(opt)) {
@@ -973,7 +975,7 @@ static int autotune_batch(gg_context *c, const gg_options *opt, const gg_job *jo
       return best;
     };
     ClassCfg base;
-    base.T = S <= 16 && !opt->input_sorted ? 16 : 32;
+    base.T = S <= 16 && !opt->input_sorted ? 8 : 32;
     base.W = 0;
     base.chunk = 2048;
     const double t_default = timeit(base);

@@ -196,10 +196,12 @@ constexpr int kWinThreads = 256;
 // carries at most about L/2 units in the last place of relative error
 constexpr int kRunMax = 32;
 
-// warps per sub-grid group chosen when the caller leaves it open
-// (measured on the 4096^2 track workload: S=8 with 2 warps per group beats 1)
-__host__ __device__ constexpr int win_default_warps(int S) {
-  return S >= 32 ? 8 : (S >= 8 ? 2 : 1);
+// warps per sub-grid group chosen when the caller leaves it open, by support
+// and tile (measured on the track and disk workloads: one-warp groups for
+// support 8 on 8-cell tiles, where their sub-grids are small enough for three
+// CTAs per SM; two warps otherwise for supports 8 and 16; four for 32)
+__host__ __device__ constexpr int win_default_warps(int S, int T) {
+  return S >= 32 ? 4 : (S >= 16 ? 2 : (S >= 8 ? (T <= 8 ? 1 : 2) : 1));
 }
 
 template <int S, int W> struct WinCfg {
@@ -720,8 +722,8 @@ static cudaError_t win_modes(const GridLaunch &g, const KParams &kp, cudaStream_
 
 // supported (support, warps per group): Q = S*S/(32 W) residues per thread
 // between 1 and 8
-static int win_warps(int S, int requested) {
-  int w = requested > 0 ? requested : win_default_warps(S);
+static int win_warps(int S, int requested, int T) {
+  int w = requested > 0 ? requested : win_default_warps(S, T);
   switch (S) {
     case 4: return 1;
     case 8: return w >= 2 ? 2 : 1;
@@ -733,7 +735,7 @@ static int win_warps(int S, int requested) {
 
 size_t window_smem_bytes(int S, int accum, int vals_f64, int T, int group_warps, int gauss) {
   const int mode = vals_f64 ? 2 : (accum == GG_ACC_COMPENSATED ? 1 : 0);
-  const int w = win_warps(S, group_warps);
+  const int w = win_warps(S, group_warps, T);
 #define GG_WSG(SV, WV, MV)                                                 \
   return gauss ? WinLayout<SV, WV, MV, true>::cta_bytes(T)                 \
                : WinLayout<SV, WV, MV, false>::cta_bytes(T)
@@ -829,7 +831,7 @@ cudaError_t launch_window(const GridLaunch &g, cudaStream_t s) {
   kp.T = g.tile;
   kp.G = g.G;
   kp.sigma = g.sigma;
-  const int w = win_warps(g.S, g.group_warps);
+  const int w = win_warps(g.S, g.group_warps, g.tile);
   switch (g.S) {
     case 4: return win_modes<4, 1>(g, kp, s);
     case 8: return w == 2 ? win_modes<8, 2>(g, kp, s) : win_modes<8, 1>(g, kp, s);
