@@ -205,6 +205,22 @@ typedef struct gg_job {
 int gg_grid_device(gg_context *ctx, const gg_options *opt, const gg_job *job,
                    void *stream);
 
+/* Degridding, the adjoint of gridding (no counterpart in the reference; it
+ * keeps the gridder's index step, tap window (-S/2, S/2] and table layout):
+ *   vals[n][p] = sum over the on-grid taps of visibility n of
+ *                grid[p][y][x] * conj(gcf entry of the tap)
+ * so that <grid(v), g> = <v, degrid(g)> for <a, b> = sum conj(a) b.  The
+ * job's fields are read as for gg_grid_device except that `out` is the grid
+ * to sample (read, out_type, opt->layout: GG_LAYOUT_PLANAR planar, every
+ * other layout interleaved) and `vals` RECEIVES npts*P values (vals_type);
+ * the table (or Gaussian) and gcf_index/n_gcf select the kernel as for
+ * gridding.  Visibilities with an oversample or table index out of range get
+ * zero and are counted (gg_read_flags()[0]).  FP32 values: plain FP32 sums,
+ * or two-sum compensated ones with GG_ACC_COMPENSATED; FP64 values: FP64.
+ * Asynchronous on `stream`; no workspace, no allocation. */
+int gg_degrid_device(gg_context *ctx, const gg_options *opt, const gg_job *job,
+                     void *stream);
+
 /* Many independent jobs in one persistent launch over a device work queue of
  * (job, uv tile) items.  All jobs share opt, S-class and types. */
 int gg_grid_batch(gg_context *ctx, const gg_options *opt, const gg_job *jobs,

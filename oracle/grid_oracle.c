@@ -256,3 +256,84 @@ void oracle_gaussian_gcf(double *gcf, double *g1, int S, int G,
   if (gcf) oracle_gcf_from_1d(gcf, g, S, G);
   if (!g1) free(g);
 }
+
+/* ---- degridding (adjoint of the gridder) --------------------------------- */
+
+typedef struct {
+  double *vals;
+  const double *grid, *uv, *gcf;
+  const int32_t *gcfinx;
+  size_t n0, n1, img_dim, gcf_dim;
+  int n_gcf, G, P;
+} degrid_job;
+
+static void degrid_range(const degrid_job *j) {
+  const long S = (long)j->gcf_dim, N = (long)j->img_dim;
+  const int G = j->G, P = j->P;
+  const size_t NN = (size_t)N * N;
+  const double *re = j->grid, *im = j->grid + (size_t)P * NN;
+  for (size_t n = j->n0; n < j->n1; n++) {
+    int main_x, main_y, sub_x, sub_y;
+    index_step(j->uv[2 * n], G, &main_x, &sub_x);
+    index_step(j->uv[2 * n + 1], G, &main_y, &sub_y);
+    int ok = sub_x >= 0 && sub_x < G && sub_y >= 0 && sub_y < G;
+    long table = 0;
+    if (ok && j->gcfinx) {
+      ok = j->gcfinx[n] >= 0 && j->gcfinx[n] < j->n_gcf;
+      table = ok ? (long)j->gcfinx[n] * G * G * S * S : 0;
+    }
+    for (int p = 0; p < P; p++) {
+      double sr = 0, si = 0;
+      if (ok) {
+        const double *w = j->gcf + 2 * (table + S * S * ((long)G * sub_y + sub_x));
+        for (long bp = 0; bp < S; bp++)
+          for (long ap = 0; ap < S; ap++) {
+            const long x = main_x + ap - S / 2 + 1, y = main_y + bp - S / 2 + 1;
+            if (x < 0 || y < 0 || x >= N || y >= N) continue;
+            const double wr = w[2 * (S * bp + ap)], wi = w[2 * (S * bp + ap) + 1];
+            const size_t c = (size_t)p * NN + (size_t)y * N + (size_t)x;
+            /* grid * conj(w) */
+            sr += re[c] * wr + im[c] * wi;
+            si += im[c] * wr - re[c] * wi;
+          }
+      }
+      j->vals[2 * (P * n + p)] = sr;
+      j->vals[2 * (P * n + p) + 1] = si;
+    }
+  }
+}
+
+static void *degrid_thread(void *arg) {
+  degrid_range((const degrid_job *)arg);
+  return NULL;
+}
+
+void oracle_degrid_pz(double *vals_out, const double *grid_planar,
+                      const double *uv, const int32_t *gcfinx, size_t npts,
+                      size_t img_dim, const double *gcf, int n_gcf,
+                      size_t gcf_dim, int gcf_grid, int pols, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if ((size_t)nthreads > npts) nthreads = npts > 0 ? (int)npts : 1;
+  degrid_job *jobs = (degrid_job *)calloc((size_t)nthreads, sizeof(degrid_job));
+  pthread_t *tid = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+  for (int t = 0; t < nthreads; t++) {
+    degrid_job *j = &jobs[t];
+    j->vals = vals_out;
+    j->grid = grid_planar;
+    j->uv = uv;
+    j->gcf = gcf;
+    j->gcfinx = gcfinx;
+    j->n0 = npts * (size_t)t / (size_t)nthreads;
+    j->n1 = npts * (size_t)(t + 1) / (size_t)nthreads;
+    j->img_dim = img_dim;
+    j->gcf_dim = gcf_dim;
+    j->n_gcf = n_gcf < 1 ? 1 : n_gcf;
+    j->G = gcf_grid;
+    j->P = pols;
+  }
+  for (int t = 1; t < nthreads; t++) pthread_create(&tid[t], NULL, degrid_thread, &jobs[t]);
+  degrid_range(&jobs[0]);
+  for (int t = 1; t < nthreads; t++) pthread_join(tid[t], NULL);
+  free(jobs);
+  free(tid);
+}

@@ -64,6 +64,24 @@ void oracle_grid_pz_wphase(double *out_planar, const double *uv,
                            const double *gcf, size_t gcf_dim, int gcf_grid,
                            int pols, int nthreads);
 
+/* Degridding, the adjoint of oracle_grid_pz_gcfinx (the reference has no
+ * degridder; this follows its gridder's conventions, grid.cu:157-191):
+ *   vals_out[n][p] = sum over the taps (a, b) in (-S/2, S/2]^2 of visibility
+ *                    n that fall on the grid of grid[p][y][x] * conj(w)
+ * with the index step, tap window and table entry w of the gridder, so that
+ * <grid_pz(v), g> = <v, degrid_pz(g)> for the complex inner product
+ * <a, b> = sum conj(a) b.  grid_planar is laid out like out_planar above
+ * (real planes, then imaginary planes); vals_out receives npts*pols complex
+ * values (re, im), OVERWRITTEN.  A visibility whose oversample index falls
+ * outside [0, gcf_grid) or whose table index (gcfinx, NULL: table 0) falls
+ * outside [0, n_gcf) gets zero.  The products are summed in the tap order
+ * b' (rows) then a' (columns), in double; nthreads split the visibilities,
+ * so the result does not depend on nthreads. */
+void oracle_degrid_pz(double *vals_out, const double *grid_planar,
+                      const double *uv, const int32_t *gcfinx, size_t npts,
+                      size_t img_dim, const double *gcf, int n_gcf,
+                      size_t gcf_dim, int gcf_grid, int pols, int nthreads);
+
 /* The index step of gridCPU_pz (grid.cu:159-163): main = floor(u),
  * sub = floorf(G*(u - floorf(u))) with the float conversions C applies.
  * Writes packed (main*G+sub) pairs like vis2ints (grid_gpu.cu:352-365). */

@@ -55,6 +55,8 @@ def lib():
                                             ctypes.c_int]
         L.oracle_grid_pz_wphase.argtypes = [_dp, _dp, _dp, _sz, _sz, _dp, _sz, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_int]
+        L.oracle_degrid_pz.argtypes = [_dp, _dp, _dp, _ip, _sz, _sz, _dp, ctypes.c_int, _sz,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_vis2ints.argtypes = [_dp, _sz, ctypes.c_int, _ip]
         L.oracle_vis2ints_gpu_formula.argtypes = [_dp, _sz, ctypes.c_int, _ip]
         L.oracle_set_bookmarks.argtypes = [_ip, _sz, ctypes.c_int, ctypes.c_int,
@@ -63,7 +65,7 @@ def lib():
                                           ctypes.c_double]
         L.oracle_gcf_from_1d.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int]
         for f in (L.oracle_grid_pz, L.oracle_grid_pz_mt, L.oracle_grid_pz_gcfinx,
-                  L.oracle_grid_pz_wphase,
+                  L.oracle_grid_pz_wphase, L.oracle_degrid_pz,
                   L.oracle_vis2ints,
                   L.oracle_vis2ints_gpu_formula, L.oracle_set_bookmarks,
                   L.oracle_gaussian_gcf, L.oracle_gcf_from_1d):
@@ -121,6 +123,32 @@ def grid_pz_gcfinx(uv, vals, gcfinx, gcfs, img_dim: int, gcf_dim: int, pols: int
     lib().oracle_grid_pz_gcfinx(_ptr(out), _ptr(uv), _ptr(vals), _ptr(idx, _ip), npts, img_dim,
                                 _ptr(tabs), n_gcf, gcf_dim, gcf_grid, pols, 0, max(1, nthreads))
     return out
+
+
+def degrid_pz(uv, grid, gcf, img_dim: int, gcf_dim: int, pols: int = 1,
+              gcf_grid: int = 8, gcfinx=None, nthreads: int = 1) -> np.ndarray:
+    """Degridding, the adjoint of grid_pz / grid_pz_gcfinx: visibility n, plane
+    p gets the sum over its on-grid taps of grid[p][y][x] * conj(w), w the
+    gridder's table entry for that tap.  ``grid`` is planar (2, P, N, N)
+    (real planes, then imaginary planes), ``gcf`` one table or a stack of
+    tables selected by ``gcfinx``.  Returns complex128 values, shape
+    (npts, P); visibilities with an oversample or table index out of range
+    get zero."""
+    uv = _as_pairs(uv)
+    tabs = _as_pairs(gcf)
+    per = gcf_grid * gcf_grid * gcf_dim * gcf_dim
+    assert tabs.shape[0] % per == 0
+    n_gcf = tabs.shape[0] // per
+    npts = uv.shape[0]
+    g = np.ascontiguousarray(grid, np.float64)
+    assert g.shape == (2, pols, img_dim, img_dim)
+    out = np.zeros((npts * pols, 2), np.float64)
+    idx = None if gcfinx is None else np.ascontiguousarray(gcfinx, np.int32)
+    assert idx is None or idx.shape == (npts,)
+    lib().oracle_degrid_pz(_ptr(out), _ptr(g), _ptr(uv),
+                           None if idx is None else _ptr(idx, _ip), npts, img_dim, _ptr(tabs),
+                           n_gcf, gcf_dim, gcf_grid, pols, max(1, nthreads))
+    return (out[:, 0] + 1j * out[:, 1]).reshape(npts, pols)
 
 
 def grid_pz_wphase(uv, vals, gcf, img_dim: int, gcf_dim: int, pols: int = 1,

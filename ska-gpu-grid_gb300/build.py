@@ -28,7 +28,7 @@ PROBE_LIB = os.path.join(HERE, "libgg_probe.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["gg_api.cu", "gg_bin.cu", "gg_scatter.cu", "gg_window.cu",
-           "gg_gather.cu", "gg_noalloc.cu", "gg_server.cu"]
+           "gg_gather.cu", "gg_noalloc.cu", "gg_server.cu", "gg_degrid.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

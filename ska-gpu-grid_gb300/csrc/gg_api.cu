@@ -1176,6 +1176,56 @@ int gg_grid_device(gg_context *ctx, const gg_options *opt, const gg_job *job,
   return grid_jobs(ctx, opt, job, 1, (cudaStream_t)stream);
 }
 
+int gg_degrid_device(gg_context *ctx, const gg_options *opt, const gg_job *job,
+                     void *stream) {
+  if (!ctx) return fail(GG_ERR_ARG, "ctx: null");
+  if (!job) return fail(GG_ERR_ARG, "job: null");
+  int st = check_options(opt);
+  if (st) return st;
+  const gg_job &J = *job;
+  if (J.gcf_dim != 4 && J.gcf_dim != 8 && J.gcf_dim != 16 && J.gcf_dim != 32)
+    return fail(GG_ERR_ARG, "degrid: gcf_dim %lld not in {4,8,16,32}", (long long)J.gcf_dim);
+  if (J.img_dim < 1 || J.img_dim > (1 << 16))
+    return fail(GG_ERR_ARG, "degrid: img_dim %lld outside 1..65536", (long long)J.img_dim);
+  if (J.npts < 0) return fail(GG_ERR_ARG, "degrid: npts < 0");
+  for (int t : {J.uv_type, J.vals_type, J.out_type})
+    if (t != GG_C64 && t != GG_C128) return fail(GG_ERR_ARG, "degrid: type %d", t);
+  if (opt->gcf_kind != GG_GCF_TABLE && opt->gcf_kind != GG_GCF_GAUSSIAN)
+    return fail(GG_ERR_ARG, "degrid: gcf_kind %d (table or Gaussian)", opt->gcf_kind);
+  const bool gauss = opt->gcf_kind == GG_GCF_GAUSSIAN;
+  if (J.npts > 0 && (!J.out || !J.uv || !J.vals || (!gauss && !J.gcf)))
+    return fail(GG_ERR_ARG, "degrid: null device pointer");
+  if (J.gcf_index && (gauss || J.n_gcf < 1 || J.n_gcf > 32768))
+    return fail(GG_ERR_ARG, "degrid: gcf_index needs a table stack of 1..32768 tables");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  GG_CUDA(cudaSetDevice(ctx->device));
+  DegridLaunch d{};
+  d.grid = J.out;
+  d.vals = const_cast<void *>(J.vals);
+  d.uv = J.uv;
+  d.gcf = gauss ? nullptr : J.gcf;
+  d.gcf_index = J.gcf_index;
+  d.npts = J.npts;
+  d.N = (int)J.img_dim;
+  d.S = (int)J.gcf_dim;
+  d.G = opt->oversample;
+  d.P = opt->polarizations;
+  d.n_gcf = J.gcf_index ? (int)J.n_gcf : 1;
+  d.uv_f64 = J.uv_type == GG_C128;
+  d.grid_f64 = J.out_type == GG_C128;
+  d.vals_f64 = J.vals_type == GG_C128;
+  d.planar = opt->layout == GG_LAYOUT_PLANAR;
+  d.gauss = gauss;
+  d.compensated = opt->accum == GG_ACC_COMPENSATED;
+  const double sg = J.gcf_sigma > 0 ? J.gcf_sigma
+                                    : (opt->gcf_sigma > 0 ? opt->gcf_sigma : J.gcf_dim / 4.0);
+  d.sigma = (float)sg;
+  d.flags = (int *)ctx->flags.p;
+  d.sm_count = ctx->sm_count;
+  GG_CUDA(launch_degrid(d, (cudaStream_t)stream));
+  return GG_OK;
+}
+
 int gg_grid_batch(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
                   int32_t njobs, void *stream) {
   if (!ctx) return fail(GG_ERR_ARG, "ctx: null");

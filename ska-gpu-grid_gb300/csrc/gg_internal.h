@@ -119,6 +119,25 @@ struct GridLaunch {
   int total_tiles;
 };
 
+// Degridding (adjoint of the gridder): one launch per job
+struct DegridLaunch {
+  const void *grid;        // device: P planes of N*N complex (grid_f64: double)
+  void *vals;              // device: npts*P complex out (vals_f64: double)
+  const void *uv;          // device: npts (u,v) pairs (uv_f64: double)
+  const void *gcf;         // device: n_gcf tables [G*G][S][S] of the values' type; null: Gaussian
+  const int *gcf_index;    // device, optional: table of each visibility
+  int64_t npts;
+  int N, S, G, P, n_gcf;
+  int uv_f64, grid_f64, vals_f64;
+  int planar;              // grid layout: planar (1) or interleaved (0)
+  int gauss;               // GCF computed on the fly (separable Gaussian)
+  int compensated;         // FP32 values: two-sum (hi, lo) lane sums
+  float sigma;
+  int *flags;
+  int sm_count;
+};
+cudaError_t launch_degrid(const DegridLaunch &d, cudaStream_t s);
+
 cudaError_t launch_scatter(const GridLaunch &g, cudaStream_t s);
 cudaError_t launch_window(const GridLaunch &g, cudaStream_t s);
 // one warp waiting on an mbarrier nobody completes (bounded-wait self-test)

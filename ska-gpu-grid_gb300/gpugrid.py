@@ -132,6 +132,7 @@ def _load():
         "gg_reserve": ([vp, P(gg_options), i64, i64, i64, i32], ctypes.c_int),
         "gg_workspace_bytes": ([vp, P(sz)], ctypes.c_int),
         "gg_grid_device": ([vp, P(gg_options), P(gg_job), vp], ctypes.c_int),
+        "gg_degrid_device": ([vp, P(gg_options), P(gg_job), vp], ctypes.c_int),
         "gg_grid_batch": ([vp, P(gg_options), P(gg_job), i32, vp], ctypes.c_int),
         "gg_read_flags": ([vp, vp, P(i32)], ctypes.c_int),
         "gg_profile_enable": ([vp, ctypes.c_int], ctypes.c_int),
@@ -355,6 +356,19 @@ class Context:
         """Grid device tensors into `out` (overwritten) on the current stream."""
         self.grid_job(opts, self.make_job(out, uv, vals, gcf, img_dim, gcf_dim,
                                           gcf_sigma=gcf_sigma), stream)
+
+    def degrid(self, opts: Options, grid, uv, vals_out, gcf, img_dim: int, gcf_dim: int,
+               stream=None, gcf_sigma: float = 0.0, gcf_index=None, n_gcf: int = 1) -> None:
+        """Degrid (the adjoint of grid): vals_out (npts*P complex, written)
+        gets, per visibility and plane, the sum over its on-grid taps of
+        grid * conj(table entry).  grid: P planes of N*N complex (planar when
+        opts.layout is LAYOUT_PLANAR, else interleaved)."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        job = self.make_job(grid, uv, vals_out, gcf, img_dim, gcf_dim, gcf_sigma=gcf_sigma,
+                            gcf_index=gcf_index, n_gcf=n_gcf)
+        _check(LIB.gg_degrid_device(self._h, ctypes.byref(opts.c()), ctypes.byref(job),
+                                    ctypes.c_void_p(s.cuda_stream)))
 
     def grid_batch(self, opts: Options, jobs: list[gg_job], stream=None) -> None:
         import torch
