@@ -93,6 +93,13 @@ WORKLOADS = {
               "with 1% outliers at 1e3; support 32, oversample 8; GCF computed "
               "on the fly")),
 }
+WORKLOADS["degrid4096"] = dict(
+    kind="degrid", N=4096, S=8, npts=1 << 22, gen="tracks", vals="c64", out="c64",
+    mode="window", accum="comp", presort=True,
+    desc=("degridding (the gridder's adjoint) of the tracks4096 visibilities from "
+          "their own 4096^2 complex64 grid: 2^22 predicted complex64 values, "
+          "support 8, oversample 8, tabulated Gaussian GCF, FP32 compensated "
+          "lane sums"))
 DEFAULT_WORKLOAD = "served10k"
 
 
@@ -952,6 +959,132 @@ def run_single(args, rank, world, local_rank, dist):
 
 
 # ---------------------------------------------------------------------------
+# degridding (the gridder's adjoint) of one job
+# ---------------------------------------------------------------------------
+def run_degrid(args, rank, world, local_rank, dist):
+    import torch
+    import gpugrid as gg
+    import oracle as O
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    w = WORKLOADS[args.workload]
+    N, S, n = w["N"], w["S"], w["npts"]
+    uv, vals, gcf = make_single(w, seed=1000 + rank)
+    ctx = gg.Context(local_rank)
+    d_uv = torch.from_numpy(uv).to(dev)
+    d_vals = torch.from_numpy(vals).to(dev)
+    d_gcf = torch.from_numpy(gcf.reshape(-1)).to(dev)
+    # the grid to sample: the workload's own visibilities gridded
+    grid = torch.empty(N * N, dtype=torch.complex64, device=dev)
+    ctx.grid(gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
+                        layout=gg.LAYOUT_INTERLEAVED), grid, d_uv, d_vals, d_gcf, N, S)
+    o = gg.Options(accum=gg.ACC_COMPENSATED, layout=gg.LAYOUT_INTERLEAVED)
+    out = torch.empty(n, dtype=torch.complex64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        ctx.degrid(o, grid, d_uv, out, d_gcf, N, S)
+    torch.cuda.synchronize()
+    flags = ctx.read_flags()
+    err = None
+    if rank == 0 and not args.no_check:
+        nchk = 1 << 18
+        g = grid.cpu().numpy()
+        planar = np.stack([g.real, g.imag]).reshape(2, 1, N, N).astype(np.float64)
+        ref = O.degrid_pz(uv[:nchk], planar, pairs(gcf), N, S, nthreads=os.cpu_count())[:, 0]
+        got = out[:nchk].cpu().numpy().astype(np.complex128)
+        err = {"max_rel": float(np.abs(got - ref).max() / np.abs(ref).max()),
+               "visibilities_checked": nchk,
+               "reference": "FP64 degridding restatement (adjoint of the gridCPU_pz "
+                            "restatement, checked by <grid(v), g> = <v, degrid(g)>)"}
+        del planar, ref
+    start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = gg.kernel_launches()
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            flush.fill_(k & 0xff)            # evict L2 (untimed)
+            start[k].record(stream)
+            with nvtx_range("gg_profiled" if k == args.steps - 1 else "gg_step"):
+                ctx.degrid(o, grid, d_uv, out, d_gcf, N, S)
+            end[k].record(stream)
+        torch.cuda.synchronize()
+    launches = gg.kernel_launches() - l0
+    times = [s_.elapsed_time(e_) for s_, e_ in zip(start, end)]
+    total_ms = max_over_ranks(sum(times), dist, dev)
+    e2e = None
+    if not args.no_e2e:
+        # host buffers through the public API: coordinates and grid copied in
+        # from pinned memory, predicted values copied back, every step
+        pin_uv = torch.from_numpy(uv).pin_memory()
+        pin_grid = grid.cpu().pin_memory()
+        pin_out = torch.empty(n, dtype=torch.complex64).pin_memory()
+        d_uv2, d_grid2 = torch.empty_like(d_uv), torch.empty_like(grid)
+        ts = []
+        for k in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            d_uv2.copy_(pin_uv, non_blocking=True)
+            d_grid2.copy_(pin_grid, non_blocking=True)
+            ctx.degrid(o, d_grid2, d_uv2, out, d_gcf, N, S)
+            pin_out.copy_(out, non_blocking=True)
+            torch.cuda.synchronize()
+            if k >= args.warmup:
+                ts.append(time.perf_counter() - t0)
+        e2e_s = max_over_ranks(sum(ts), dist, dev)
+        e2e = {"value": round(replica_rate(n * args.steps, world, e2e_s), 3), "unit": "Mvis/s",
+               "h2d_bytes_per_step": int(pin_uv.numel() * 8 + pin_grid.numel() * 8),
+               "d2h_bytes_per_step": int(n * 8),
+               "ms_per_step": round(1e3 * e2e_s / args.steps, 4),
+               "api": "gpugrid.Context.degrid over gg_degrid_device, pinned host buffers"}
+    if rank != 0:
+        return None
+    value = replica_rate(n * args.steps, world, total_ms / 1e3)
+    mean_ms = statistics.mean(times)
+    alg = n * (16 + 8) + N * N * 8       # coordinates in, values out, grid read once
+    # CPU baseline: the oracle degridder over all host threads on a prefix
+    threads = os.cpu_count() or 1
+    g = grid.cpu().numpy()
+    planar = np.stack([g.real, g.imag]).reshape(2, 1, N, N).astype(np.float64)
+    m = 1 << 16
+    while True:
+        t0 = time.perf_counter()
+        O.degrid_pz(uv[:m], planar, pairs(gcf), N, S, nthreads=threads)
+        cs = time.perf_counter() - t0
+        if cs * 4 > args.cpu_budget or m >= n:
+            break
+        m = min(n, m * 4)
+    res = {
+        "metric": "degridded Mvis/s (predicted visibilities per second)",
+        "value": round(value, 3), "unit": "Mvis/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generators with the workload's shapes)",
+        "config": {"workload": f"{args.workload}: {w['desc']}",
+                   "l2": "flushed before every timed step (256 MiB write)",
+                   "img_dim": N, "gcf_dim": S, "oversample": 8, "visibilities": n,
+                   "parallelism": f"replicas x{world}"},
+        "tap_reads_per_s": round(value * 1e6 * S * S, 1),
+        "accuracy": err, "flags": flags,
+        "roofline": roofline("degrid_kernel", alg, mean_ms, f"degrid_{args.workload}",
+                             None, local_rank),
+        "cpu_baseline": {"value": round(m / cs / 1e6, 4), "unit": "Mvis/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"first {m} visibilities ({cs:.1f} s), the degridding "
+                                   f"restatement over {threads} threads"},
+        "e2e": e2e, "gpu_launches": int(launches),
+    }
+    clocks = clk.summary()
+    if clocks:
+        res["clocks"] = clocks
+    return res
+
+
+# ---------------------------------------------------------------------------
 # reference arm: the reference CPU gridder on the host cores
 # ---------------------------------------------------------------------------
 def run_reference(args, rank, world):
@@ -959,6 +1092,9 @@ def run_reference(args, rank, world):
         return None
     import oracle as O
     w = WORKLOADS[args.workload]
+    if w["kind"] == "degrid":
+        return {"impl": "reference",
+                "unavailable": "the reference has no degridder (it grids only)"}
     threads = os.cpu_count() or 1
     if w["kind"] == "single":
         uv, vals, gcf = make_single(w, seed=1000)
@@ -1055,7 +1191,8 @@ def main():
             td.init_process_group("nccl")
             dist = td
         kind = WORKLOADS[args.workload]["kind"]
-        fn = {"served": run_served, "batch": run_batch, "single": run_single}[kind]
+        fn = {"served": run_served, "batch": run_batch, "single": run_single,
+              "degrid": run_degrid}[kind]
         res = fn(args, rank, world, local_rank, dist)
         if dist:
             dist.destroy_process_group()

@@ -7,11 +7,14 @@
 //
 // and <grid(v), g> = <v, degrid(g)> for <a, b> = sum conj(a) b.
 //
-// Each visibility is summed by the lanes of one warp (S >= 8: all 32 lanes,
-// S^2/32 taps each; S = 4: half a warp, one tap each), so no atomics and no
-// binning are needed: a lane's taps of one row are contiguous cells, which
-// makes the grid reads of a warp coalesced row segments, and consecutive
-// visibilities on a uv track read overlapping footprints through L1/L2.
+// Each visibility is summed by S lanes, one footprint column each (32/S
+// visibilities per warp), so no atomics and no binning are needed: the lanes
+// of a visibility read contiguous cells of one row per step, and
+// consecutive visibilities on a uv track read overlapping footprints
+// through L1/L2.  S lanes rather than a whole warp per visibility: the
+// per-visibility work (index step, reduction) is spread over S taps per lane
+// (a whole warp on a support-8 visibility measured 330 warp instructions per
+// visibility, two taps per lane).
 // FP32 values: plain FP32 sums, or with GG_ACC_COMPENSATED a two-sum (hi, lo)
 // pair per lane that the warp reduction carries; FP64 values: FP64 sums.
 #include <type_traits>
@@ -82,12 +85,11 @@ template <typename VT, bool COMP> struct LaneSum {
 };
 
 template <int S, typename VT, typename GT, int GK, bool COMP>
-__global__ void __launch_bounds__(256, 2) degrid_kernel(DegridLaunch d) {
+__global__ void __launch_bounds__(256, 4) degrid_kernel(DegridLaunch d) {
   using VT2 = typename vec2_of<VT>::type;
   constexpr int TT = S * S;
-  constexpr int LPV = TT >= 32 ? 32 : TT;  // lanes per visibility
-  constexpr int VPW = 32 / LPV;            // visibilities per warp
-  constexpr int TPL = TT / LPV;            // taps per lane
+  constexpr int LPV = S;        // lanes per visibility: one footprint column each
+  constexpr int VPW = 32 / LPV; // visibilities per warp
   __shared__ float g1[GK == 1 ? 64 * S : 1];
   if constexpr (GK == 1) {
     gauss_fill(g1, S, d.G, d.sigma, threadIdx.x, blockDim.x);
@@ -113,21 +115,22 @@ __global__ void __launch_bounds__(256, 2) degrid_kernel(DegridLaunch d) {
       if (!ok && sl == 0) atomicAdd(&d.flags[FLAG_INDEX], 1);
     }
     const VT2 *w = tabs && ok ? tabs + ((size_t)tab * d.G * d.G + (size_t)sy * d.G + sx) * TT : tabs;
+    // this lane's column of the footprint
+    const int ap = sl, x = mx + ap - S / 2 + 1;
+    const bool xin = ok && (unsigned)x < (unsigned)d.N;
     for (int p = 0; p < d.P; ++p) {
       LaneSum<VT, COMP> sr, si;
-      if (ok) {
+      if (xin) {
 #pragma unroll 8
-        for (int k = 0; k < TPL; ++k) {
-          const int t = sl + k * LPV;
-          const int ap = t % S, bp = t / S;
-          const int x = mx + ap - S / 2 + 1, y = my + bp - S / 2 + 1;
-          if ((unsigned)x < (unsigned)d.N && (unsigned)y < (unsigned)d.N) {
+        for (int bp = 0; bp < S; ++bp) {
+          const int y = my + bp - S / 2 + 1;
+          if ((unsigned)y < (unsigned)d.N) {
             VT wr, wi;
             if constexpr (GK == 1) {
               wr = (VT)(g1[sx * S + ap] * g1[sy * S + bp]);
               wi = (VT)0;
             } else {
-              const VT2 e = __ldg(w + t);
+              const VT2 e = __ldg(w + bp * S + ap);
               wr = e.x;
               wi = e.y;
             }
@@ -185,10 +188,10 @@ cudaError_t degrid_types(const DegridLaunch &d, unsigned blocks, cudaStream_t s)
 
 cudaError_t launch_degrid(const DegridLaunch &d, cudaStream_t s) {
   if (d.npts <= 0) return cudaSuccess;
-  const int vpw = d.S >= 8 ? 1 : 2;
+  const int vpw = 32 / d.S;
   const int64_t warps = (d.npts + vpw - 1) / vpw;
   const int64_t b = (warps + 7) / 8;
-  const int64_t cap = (int64_t)d.sm_count * 8;  // 8 resident CTAs of 8 warps per SM
+  const int64_t cap = (int64_t)d.sm_count * 4;  // resident CTAs (64 registers)
   const unsigned blocks = (unsigned)(b < 1 ? 1 : (b > cap ? cap : b));
   switch (d.S) {
     case 4: return degrid_types<4>(d, blocks, s);
