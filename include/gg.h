@@ -221,6 +221,18 @@ int gg_grid_device(gg_context *ctx, const gg_options *opt, const gg_job *job,
 int gg_degrid_device(gg_context *ctx, const gg_options *opt, const gg_job *job,
                      void *stream);
 
+/* Grid -> dirty image, in place: every one of the `pols` planes of an
+ * interleaved N*N complex grid (grid_type GG_C64 / GG_C128) becomes
+ *   image[m][l] = sum_{v,u} grid[v][u]
+ *                 * exp(+2 pi i ((u-N/2)(l-N/2) + (v-N/2)(m-N/2)) / N)
+ * (zero spatial frequency at cell (N/2, N/2), image centre at pixel
+ * (N/2, N/2), no normalisation); N even, at most 32768.  No counterpart in
+ * the reference.  Uses cuFFT, loaded at first use (GG_ERR_CUDA if it cannot
+ * be); plans a transform per call and synchronises `stream`.  After an
+ * error the grid's contents are unspecified. */
+int gg_grid_to_image(gg_context *ctx, void *grid, int64_t img_dim, int32_t pols,
+                     int32_t grid_type, void *stream);
+
 /* Many independent jobs in one persistent launch over a device work queue of
  * (job, uv tile) items.  All jobs share opt, S-class and types. */
 int gg_grid_batch(gg_context *ctx, const gg_options *opt, const gg_job *jobs,

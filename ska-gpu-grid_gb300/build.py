@@ -28,7 +28,7 @@ PROBE_LIB = os.path.join(HERE, "libgg_probe.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["gg_api.cu", "gg_bin.cu", "gg_scatter.cu", "gg_window.cu",
-           "gg_gather.cu", "gg_noalloc.cu", "gg_server.cu", "gg_degrid.cu"]
+           "gg_gather.cu", "gg_noalloc.cu", "gg_server.cu", "gg_degrid.cu", "gg_image.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -93,7 +93,7 @@ def build(force: bool = False, debug: bool = False, verbose: bool = False) -> st
     if (force or jobs or not os.path.exists(LIB) or not os.path.exists(stamp)
             or open(stamp).read() != link_tag):
         cmd = [nv, "-shared", "-o", LIB + ".tmp"] + objs + ARCH + [
-            "-cudart", "shared", "-Xlinker", "-soname=libgg.so"]
+            "-cudart", "shared", "-ldl", "-Xlinker", "-soname=libgg.so"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -1226,6 +1226,24 @@ int gg_degrid_device(gg_context *ctx, const gg_options *opt, const gg_job *job,
   return GG_OK;
 }
 
+int gg_grid_to_image(gg_context *ctx, void *grid, int64_t img_dim, int32_t pols,
+                     int32_t grid_type, void *stream) {
+  if (!ctx) return fail(GG_ERR_ARG, "ctx: null");
+  if (!grid) return fail(GG_ERR_ARG, "grid: null");
+  if (img_dim < 2 || img_dim > (1 << 15) || (img_dim & 1))
+    return fail(GG_ERR_ARG, "image: img_dim %lld must be even, 2..32768", (long long)img_dim);
+  if (pols < 1 || pols > kMaxPols) return fail(GG_ERR_ARG, "image: pols %d", pols);
+  if (grid_type != GG_C64 && grid_type != GG_C128)
+    return fail(GG_ERR_ARG, "image: grid_type %d", grid_type);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  GG_CUDA(cudaSetDevice(ctx->device));
+  std::string err;
+  if (image_inverse_fft(grid, img_dim, pols, grid_type == GG_C128, ctx->sm_count,
+                        (cudaStream_t)stream, err))
+    return fail(GG_ERR_CUDA, "image: %s", err.c_str());
+  return GG_OK;
+}
+
 int gg_grid_batch(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
                   int32_t njobs, void *stream) {
   if (!ctx) return fail(GG_ERR_ARG, "ctx: null");

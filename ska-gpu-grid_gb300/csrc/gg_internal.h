@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "gg_types.h"
 
 namespace gg {
@@ -137,6 +139,10 @@ struct DegridLaunch {
   int sm_count;
 };
 cudaError_t launch_degrid(const DegridLaunch &d, cudaStream_t s);
+// centred inverse 2-D FFT of P interleaved planes in place (cuFFT, loaded at
+// first use); 0 on success, else a message in err.  Synchronises s.
+int image_inverse_fft(void *grid, int64_t N, int P, bool f64, int sm_count, cudaStream_t s,
+                      std::string &err);
 
 cudaError_t launch_scatter(const GridLaunch &g, cudaStream_t s);
 cudaError_t launch_window(const GridLaunch &g, cudaStream_t s);

@@ -133,6 +133,8 @@ def _load():
         "gg_workspace_bytes": ([vp, P(sz)], ctypes.c_int),
         "gg_grid_device": ([vp, P(gg_options), P(gg_job), vp], ctypes.c_int),
         "gg_degrid_device": ([vp, P(gg_options), P(gg_job), vp], ctypes.c_int),
+        "gg_grid_to_image": ([vp, vp, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, vp],
+                             ctypes.c_int),
         "gg_grid_batch": ([vp, P(gg_options), P(gg_job), i32, vp], ctypes.c_int),
         "gg_read_flags": ([vp, vp, P(i32)], ctypes.c_int),
         "gg_profile_enable": ([vp, ctypes.c_int], ctypes.c_int),
@@ -369,6 +371,15 @@ class Context:
                             gcf_index=gcf_index, n_gcf=n_gcf)
         _check(LIB.gg_degrid_device(self._h, ctypes.byref(opts.c()), ctypes.byref(job),
                                     ctypes.c_void_p(s.cuda_stream)))
+
+    def grid_to_image(self, grid, img_dim: int, pols: int = 1, stream=None) -> None:
+        """In place: each of the `pols` interleaved N*N complex planes of the
+        device tensor `grid` becomes its dirty image (centred inverse 2-D
+        DFT, no normalisation; N even).  Synchronises the stream."""
+        import torch
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _check(LIB.gg_grid_to_image(self._h, ctypes.c_void_p(grid.data_ptr()), img_dim, pols,
+                                    _ttype(grid), ctypes.c_void_p(s.cuda_stream)))
 
     def grid_batch(self, opts: Options, jobs: list[gg_job], stream=None) -> None:
         import torch

@@ -143,6 +143,7 @@ def test_null_arguments_rejected():
     assert gg.LIB.gg_default_options(None) == gg.ERR_ARG
     assert gg.LIB.gg_grid_device(None, None, None, None) == gg.ERR_ARG
     assert gg.LIB.gg_degrid_device(None, None, None, None) == gg.ERR_ARG
+    assert gg.LIB.gg_grid_to_image(None, None, 64, 1, gg.C64, None) == gg.ERR_ARG
     assert gg.LIB.gg_read_flags(None, None, None) == gg.ERR_ARG
     o = gg.Options().c()
     assert gg.LIB.gg_grid_host(ctypes.byref(o), 0, None, 0, None, 0, None, 1, 8,
