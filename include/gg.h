@@ -169,6 +169,13 @@ int gg_destroy(gg_context *ctx);
  * allocation-failure paths. */
 int gg_selftest_wait_timeout(gg_context *ctx, void *stream);
 int gg_debug_inject_alloc_failures(int32_t count);
+/* Test hook for the reporting of device-side failures: the next `count`
+ * served batches and allocation-free calls get the flag bits `bits`
+ * (GG_DEVFLAG_*) raised in their device flag word by a one-thread kernel
+ * enqueued after their gridding kernels and before their flags are read
+ * back -- as if a kernel had raised them.  No fault and no device wait is
+ * involved.  bits 0 switches it off. */
+int gg_debug_inject_device_flags(int32_t bits, int32_t count);
 
 /* Pre-size the context's device workspace for jobs up to these sizes so that
  * later calls allocate nothing (needed before CUDA-graph capture). */
@@ -254,9 +261,12 @@ int gg_plan_read_flags(gg_plan *plan, void *stream, int32_t flags[4]);
 int gg_plan_destroy(gg_plan *plan);
 
 /* Counters of the last completed calls on this context (synchronises the
- * stream): [0] visibilities dropped because their oversample index fell
- * outside [0,G) (u not float-representable right below an integer),
- * [1] bounded-wait timeouts, [2] unsorted input detected. */
+ * stream, then clears them): [0] visibilities dropped because their
+ * oversample index fell outside [0,G) (u not float-representable right below
+ * an integer), [1] bounded-wait timeouts, [2] unsorted input detected (the
+ * call gridded nothing), [3] an internal bounds check failed.
+ * ctx NULL: the counters of the last gg_grid_device_noalloc call on the
+ * current device (not cleared; the next such call clears them). */
 int gg_read_flags(gg_context *ctx, void *stream, int32_t flags[4]);
 
 /* Profiling (the reference's getElapsed event timer, grid_gpu.cu:38-44, made
@@ -333,9 +343,21 @@ typedef struct gg_request {
   int64_t reserved[3];
 } gg_request;
 
+/* device flag bits of a served batch (gg_result.device_flags) */
+#define GG_DEVFLAG_INDEX 1    /* visibilities dropped: oversample or table
+                                 index out of range (status stays GG_OK)   */
+#define GG_DEVFLAG_TIMEOUT 2  /* a bounded device wait expired: the batch's
+                                 requests fail with GG_ERR_TIMEOUT          */
+#define GG_DEVFLAG_UNSORTED 4 /* input declared tile-sorted was not: the
+                                 requests fail with GG_ERR_UNSORTED         */
+#define GG_DEVFLAG_BOUNDS 8   /* an internal bounds check failed: the
+                                 requests fail with GG_ERR_STATE            */
+
 typedef struct gg_result {
   int32_t status;     /* GG_OK or GG_ERR_*                                  */
-  int32_t reserved0;
+  int32_t device_flags; /* GG_DEVFLAG_* raised by the batch the request was
+                         gridded in (the flags are per batch: a flag may come
+                         from another request of the same batch)         */
   double latency_s;   /* arrival -> grid ready                              */
   double queue_s;     /* arrival -> launch                                  */
   void *device_out;   /* GG_REQ_KEEP_RESIDENT: the grid on the device       */
@@ -376,22 +398,29 @@ int gg_server_destroy(gg_server *srv);
 /* ---- allocation-free moving window -------------------------------------
  * No counterpart in the reference.  Grids one job like gg_grid_device with
  * the moving-window method, but every scratch buffer (tile histogram,
- * bookmarks, sorted visibilities, work queue, counters) comes from a fixed
- * array compiled into libgg.so instead of an allocation.  It is for callers
- * that must not allocate device memory while they run: a real-time ingest
- * that reserves all of its GPU memory at start-up because cudaMalloc can
- * block on the device or fail mid-observation, or a plugin inside a host
- * framework that owns the device memory pool.  The caller passes inputs and
- * outputs (device pointers) as for gg_grid_device.
- * Limits: npts <= 262144; at most 16384 uv tiles (img_dim <= 4096 at the
- * default 32-cell tile); one polarisation; complex64 values.  Larger jobs are
- * rejected with GG_ERR_ARG.  The array (about 9 MiB) stays resident on every
- * GPU that loads libgg.so until the process exits.
+ * bookmarks, sorted visibilities, work queue, merge slots, counters) comes
+ * from a fixed array compiled into libgg.so instead of an allocation.  It is
+ * for callers that must not allocate device memory while they run: a
+ * real-time ingest that reserves all of its GPU memory at start-up because
+ * cudaMalloc can block on the device or fail mid-observation, or a plugin
+ * inside a host framework that owns the device memory pool.  The caller
+ * passes inputs and outputs (device pointers) as for gg_grid_device.
+ * Limits, each rejected with GG_ERR_ARG: npts <= 262144; at most 16384 uv
+ * tiles (img_dim <= 4096 at the default 32-cell tile); tile 0 (= 32) or a
+ * power of two in 16..256; oversample a power of two in 1..64; one
+ * polarisation; complex64 values; GCF TABLE of at most 65536 taps (G*G*S*S,
+ * e.g. G 8 with S 32) or GAUSSIAN; no per-visibility tables (gcf_index).  The
+ * array (12206336 bytes, 11.6 MiB) stays resident on every GPU that loads
+ * libgg.so until the process exits.
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current: make that first call
- * before any stream capture.  All calls share the array and clear what must
- * start at zero; calls that overlap on the GPU (other streams or threads)
- * race on it. */
+ * before any stream capture.  A call enqueues kernels and memsets only; it
+ * reads no host memory on the stream and does not wait for it.  All calls
+ * share the array and clear what must start at zero; calls that overlap on
+ * the GPU (other streams or threads) race on it.  Device-side failures
+ * (unsorted input declared sorted, an expired bounded wait, dropped
+ * visibilities) are read with gg_read_flags(NULL, stream, flags) after the
+ * call. */
 int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
                            void *stream);
 

@@ -31,6 +31,7 @@ typedef struct {
   const int32_t *gcfinx; /* per-visibility table index (NULL: table 0) */
   int n_gcf;
   int wphase; /* COMPUTE_GCF phase factor instead of the table */
+  int mag;    /* magnitude sums |val|*|w| into out (one plane set) */
 } band_job;
 
 /* The reference GPU scatter kernel's COMPUTE_GCF factor (grid_gpu.cu:103-108,
@@ -90,7 +91,10 @@ static void grid_band(const band_job *j) {
         double i2 = j->wphase ? wi : g[2 * (S * b + a) + 1];
         for (int p = 0; p < P; p++) {
           size_t cell = (size_t)x + (size_t)N * y + (size_t)p * N * N;
-          if (j->debug1) {
+          if (j->mag) {
+            const double r1 = j->vals[2 * (P * n + p)], i1 = j->vals[2 * (P * n + p) + 1];
+            out1[cell] += sqrt(r1 * r1 + i1 * i1) * sqrt(r2 * r2 + i2 * i2);
+          } else if (j->debug1) {
             out1[cell] += 1;
             out2[cell] += (double)n;
           } else {
@@ -108,7 +112,7 @@ void oracle_grid_pz(double *out_planar, const double *uv, const double *vals,
                     size_t npts, size_t img_dim, const double *gcf,
                     size_t gcf_dim, int gcf_grid, int pols, int debug1) {
   band_job j = {out_planar, uv, vals, gcf, npts, img_dim, gcf_dim,
-                gcf_grid, pols, debug1, 0, (long)img_dim, NULL, 1, 0};
+                gcf_grid, pols, debug1, 0, (long)img_dim, NULL, 1, 0, 0};
   grid_band(&j);
 }
 
@@ -129,6 +133,18 @@ static void grid_mt(double *out_planar, const double *uv, const double *vals,
                     const int32_t *gcfinx, size_t npts, size_t img_dim,
                     const double *gcf, int n_gcf, size_t gcf_dim, int gcf_grid,
                     int pols, int debug1, int wphase, int nthreads);
+static void grid_mt_mode(double *out_planar, const double *uv, const double *vals,
+                         const int32_t *gcfinx, size_t npts, size_t img_dim,
+                         const double *gcf, int n_gcf, size_t gcf_dim, int gcf_grid,
+                         int pols, int debug1, int wphase, int mag, int nthreads);
+
+void oracle_grid_mag_pz(double *mag, const double *uv, const double *vals,
+                        const int32_t *gcfinx, size_t npts, size_t img_dim,
+                        const double *gcf, int n_gcf, size_t gcf_dim, int gcf_grid,
+                        int pols, int wphase, int nthreads) {
+  grid_mt_mode(mag, uv, vals, gcfinx, npts, img_dim, gcf, n_gcf, gcf_dim, gcf_grid, pols, 0,
+               wphase, 1, nthreads);
+}
 
 void oracle_grid_pz_gcfinx(double *out_planar, const double *uv,
                            const double *vals, const int32_t *gcfinx,
@@ -151,6 +167,14 @@ static void grid_mt(double *out_planar, const double *uv, const double *vals,
                     const int32_t *gcfinx, size_t npts, size_t img_dim,
                     const double *gcf, int n_gcf, size_t gcf_dim, int gcf_grid,
                     int pols, int debug1, int wphase, int nthreads) {
+  grid_mt_mode(out_planar, uv, vals, gcfinx, npts, img_dim, gcf, n_gcf, gcf_dim, gcf_grid, pols,
+               debug1, wphase, 0, nthreads);
+}
+
+static void grid_mt_mode(double *out_planar, const double *uv, const double *vals,
+                         const int32_t *gcfinx, size_t npts, size_t img_dim,
+                         const double *gcf, int n_gcf, size_t gcf_dim, int gcf_grid,
+                         int pols, int debug1, int wphase, int mag, int nthreads) {
   if (nthreads < 1) nthreads = 1;
   if ((size_t)nthreads > img_dim) nthreads = (int)img_dim;
   band_job *jobs = (band_job *)calloc((size_t)nthreads, sizeof(band_job));
@@ -160,7 +184,7 @@ static void grid_mt(double *out_planar, const double *uv, const double *vals,
                   gcf_grid, pols, debug1,
                   (long)(img_dim * (size_t)t / (size_t)nthreads),
                   (long)(img_dim * (size_t)(t + 1) / (size_t)nthreads),
-                  gcfinx, n_gcf, wphase};
+                  gcfinx, n_gcf, wphase, mag};
     jobs[t] = j;
   }
   char *joined = (char *)calloc((size_t)nthreads, 1);

@@ -64,6 +64,21 @@ void oracle_grid_pz_wphase(double *out_planar, const double *uv,
                            const double *gcf, size_t gcf_dim, int gcf_grid,
                            int pols, int nthreads);
 
+/* Per-cell magnitude sums for the forward-error metric of the tests and the
+ * benchmark (no counterpart in the reference):
+ *   mag[p][y][x] = sum of |val| * |w| over exactly the visibilities and taps
+ * that gridCPU_pz adds into cell (x, y) of plane p (same index step, tap
+ * window, table selection -- gcfinx NULL: table 0 -- and COMPUTE_GCF factor
+ * when wphase is nonzero).  |grid - oracle| / mag at a cell is the forward
+ * error of that cell's sum relative to the magnitudes summed there, the
+ * quantity the rounding-error bound of a floating-point sum is stated in; it
+ * stays meaningful at cells where the sum cancels.  mag holds
+ * pols*img_dim^2 doubles, ACCUMULATED (+=). */
+void oracle_grid_mag_pz(double *mag, const double *uv, const double *vals,
+                        const int32_t *gcfinx, size_t npts, size_t img_dim,
+                        const double *gcf, int n_gcf, size_t gcf_dim, int gcf_grid,
+                        int pols, int wphase, int nthreads);
+
 /* Degridding, the adjoint of oracle_grid_pz_gcfinx (the reference has no
  * degridder; this follows its gridder's conventions, grid.cu:157-191):
  *   vals_out[n][p] = sum over the taps (a, b) in (-S/2, S/2]^2 of visibility

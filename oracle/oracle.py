@@ -55,6 +55,8 @@ def lib():
                                             ctypes.c_int]
         L.oracle_grid_pz_wphase.argtypes = [_dp, _dp, _dp, _sz, _sz, _dp, _sz, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_int]
+        L.oracle_grid_mag_pz.argtypes = [_dp, _dp, _dp, _ip, _sz, _sz, _dp, ctypes.c_int, _sz,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_degrid_pz.argtypes = [_dp, _dp, _dp, _ip, _sz, _sz, _dp, ctypes.c_int, _sz,
                                        ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.oracle_vis2ints.argtypes = [_dp, _sz, ctypes.c_int, _ip]
@@ -65,7 +67,7 @@ def lib():
                                           ctypes.c_double]
         L.oracle_gcf_from_1d.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int]
         for f in (L.oracle_grid_pz, L.oracle_grid_pz_mt, L.oracle_grid_pz_gcfinx,
-                  L.oracle_grid_pz_wphase, L.oracle_degrid_pz,
+                  L.oracle_grid_pz_wphase, L.oracle_grid_mag_pz, L.oracle_degrid_pz,
                   L.oracle_vis2ints,
                   L.oracle_vis2ints_gpu_formula, L.oracle_set_bookmarks,
                   L.oracle_gaussian_gcf, L.oracle_gcf_from_1d):
@@ -122,6 +124,31 @@ def grid_pz_gcfinx(uv, vals, gcfinx, gcfs, img_dim: int, gcf_dim: int, pols: int
     out = np.zeros((2, pols, img_dim, img_dim), np.float64)
     lib().oracle_grid_pz_gcfinx(_ptr(out), _ptr(uv), _ptr(vals), _ptr(idx, _ip), npts, img_dim,
                                 _ptr(tabs), n_gcf, gcf_dim, gcf_grid, pols, 0, max(1, nthreads))
+    return out
+
+
+def grid_mag(uv, vals, gcf, img_dim: int, gcf_dim: int, pols: int = 1,
+             gcf_grid: int = 8, gcfinx=None, wphase: bool = False,
+             nthreads: int = 1) -> np.ndarray:
+    """Per-cell magnitude sums sum |val| * |w| over the additions gridCPU_pz
+    makes into each cell (same taps, tables and COMPUTE_GCF factor): the
+    denominator of the per-cell forward error.  ``gcf`` is one table or a
+    stack selected by ``gcfinx``.  Returns (P, N, N) float64."""
+    uv = _as_pairs(uv)
+    vals = _as_pairs(vals)
+    tabs = _as_pairs(gcf)
+    per = gcf_grid * gcf_grid * gcf_dim * gcf_dim
+    assert tabs.shape[0] % per == 0
+    n_gcf = tabs.shape[0] // per
+    npts = uv.shape[0]
+    assert vals.shape[0] == npts * pols
+    idx = None if gcfinx is None else np.ascontiguousarray(gcfinx, np.int32)
+    assert idx is None or idx.shape == (npts,)
+    out = np.zeros((pols, img_dim, img_dim), np.float64)
+    lib().oracle_grid_mag_pz(_ptr(out), _ptr(uv), _ptr(vals),
+                             None if idx is None else _ptr(idx, _ip), npts, img_dim,
+                             _ptr(tabs), n_gcf, gcf_dim, gcf_grid, pols, int(wphase),
+                             max(1, nthreads))
     return out
 
 

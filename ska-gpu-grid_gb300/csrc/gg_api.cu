@@ -75,6 +75,17 @@ bool injected_alloc_failure() {
   return false;
 }
 
+// gg_debug_inject_device_flags: flag bits and how many more served batches /
+// allocation-free calls receive them
+static std::mutex g_inject_mu;
+static int g_inject_bits = 0, g_inject_count = 0;
+int injected_device_flags() {
+  std::lock_guard<std::mutex> lk(g_inject_mu);
+  if (g_inject_count <= 0) return 0;
+  --g_inject_count;
+  return g_inject_bits;
+}
+
 struct DevBuf {
   void *p = nullptr;
   size_t n = 0;
@@ -222,6 +233,11 @@ struct Plan {
   std::vector<size_t> hgcf_copy;  // per job (class order): index of its copy
   std::vector<GcfCopy> gcf_copies;
   std::vector<size_t> hgcf_off;
+  // FP64 merge slots per support class (compensated FP32 moving window into
+  // complex64 grids): offsets of the slots and their descriptors, slots and
+  // double2 values per slot (0 slots: none)
+  size_t o_merge[kMaxClasses] = {}, o_mdesc[kMaxClasses] = {};
+  int merge_cap[kMaxClasses] = {}, merge_cells[kMaxClasses] = {};
   // workspace carve (offsets into the device workspace)
   size_t o_jobs, o_bin, o_visb, o_tileb, o_class, o_packed, o_key, o_bm,
       o_cursor, o_scan, o_sidx, o_svals, o_order, o_items, o_kept, o_lo,
@@ -274,6 +290,8 @@ struct gg_context {
   int prof_recorded = 0;
   cudaEvent_t prof[4] = {nullptr, nullptr, nullptr, nullptr};
 };
+
+int *gg::context_flags(gg_context *c) { return (int *)c->flags.p; }
 
 static int ctx_init(gg_context *c, int device) {
   c->device = device;
@@ -599,6 +617,30 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
     }
     pl.o_gcf_flags = take(sizeof(int) * (pl.gcf_copies.size() + 1));
   }
+  // merge slots: classes in ascending support, like cfgs
+  if (mode == GG_MODE_WINDOW && pl.accum == GG_ACC_COMPENSATED && !pl.vals_f64) {
+    int ci = 0;
+    for (const auto &kv : cfgs) {
+      const int S = kv.first;
+      int64_t cvis = 0, ctiles = 0;
+      bool c64 = false;
+      for (int j = 0; j < njobs; ++j)
+        if (jobs[j].gcf_dim == S) {
+          cvis += jobs[j].npts;
+          const int64_t ntx = (jobs[j].img_dim + kv.second.T - 1) / kv.second.T;
+          ctiles += ntx * ntx * (jobs[j].gcf_index ? jobs[j].n_gcf : 1);
+          c64 |= jobs[j].out_type == GG_C64;
+        }
+      if (c64 && ci < kMaxClasses) {
+        const int R = kv.second.T + S - 1;
+        pl.merge_cap[ci] = merge_slot_cap(cvis, kv.second.chunk, ctiles);
+        pl.merge_cells[ci] = pl.P * R * R;
+        pl.o_merge[ci] = take(sizeof(double2) * (size_t)pl.merge_cap[ci] * pl.merge_cells[ci]);
+        pl.o_mdesc[ci] = take(sizeof(int2) * (size_t)pl.merge_cap[ci]);
+      }
+      ++ci;
+    }
+  }
   pl.ws_bytes = off;
 
   // host tables in class order
@@ -841,13 +883,25 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
   }
 
   if (pl.mode == GG_MODE_WINDOW) {
-    GG_CUDA(cudaMemsetAsync(flags + 8, 0, 8 * sizeof(int), s));
+    // item counters [8, 12), item claims [12, 16), merge slots taken [16, 20)
+    GG_CUDA(cudaMemsetAsync(flags + 8, 0, 12 * sizeof(int), s));
     WorkItem *items = (WorkItem *)(ws + pl.o_items);
     ClassChunks chunks;
-    for (int ci = 0; ci < kMaxClasses; ++ci)
+    ClassSlots slots{};
+    for (int ci = 0; ci < kMaxClasses; ++ci) {
       chunks.c[ci] = ci < (int)pl.classes.size() ? pl.classes[ci].chunk : pl.chunk;
+      if (pl.merge_cap[ci] > 0) {
+        slots.m[ci].base = (double2 *)(ws + pl.o_merge[ci]);
+        slots.m[ci].desc = (int2 *)(ws + pl.o_mdesc[ci]);
+        slots.m[ci].cap = pl.merge_cap[ci];
+        slots.m[ci].cells = pl.merge_cells[ci];
+      }
+    }
     GG_CUDA(launch_make_items((const int *)(ws + pl.o_bm), dtileb, dclass, pl.njobs,
-                              pl.total_tiles, chunks, items, pl.class_cap, flags + 8, s));
+                              pl.total_tiles, chunks, items, pl.class_cap, flags + 8, s,
+                              djobs, &slots, flags + 16, flags));
+    for (int ci = 0; ci < kMaxClasses; ++ci)
+      GG_CUDA(launch_merge_zero(slots.m[ci], flags + 16 + ci, sm_count, s));
     if (prof) GG_CUDA(cudaEventRecord(prof->ev[1], s));
     for (size_t ci = 0; ci < pl.classes.size(); ++ci) {
       const auto &cl = pl.classes[ci];
@@ -861,7 +915,10 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
       if (side) GG_CUDA(cudaStreamWaitEvent(s, aux->done[ci], 0));
       g.item_next = flags + 12 + ci;
       g.max_items = pl.class_cap;
+      g.merge = slots.m[ci];
       GG_CUDA(launch_window(g, s));
+      GG_CUDA(launch_merge_finalize(slots.m[ci], flags + 16 + ci, djobs, cl.S, cl.T, pl.P,
+                                    sm_count, s));
     }
     if (prof) GG_CUDA(cudaEventRecord(prof->ev[2], s));
   } else if (pl.mode == GG_MODE_GATHER) {
@@ -1071,6 +1128,14 @@ int gg_debug_inject_alloc_failures(int32_t count) {
   return GG_OK;
 }
 
+int gg_debug_inject_device_flags(int32_t bits, int32_t count) {
+  if (count < 0 || (bits & ~0xf)) return fail(GG_ERR_ARG, "bits outside 0..15 or count < 0");
+  std::lock_guard<std::mutex> lk(g_inject_mu);
+  g_inject_bits = bits;
+  g_inject_count = bits ? count : 0;
+  return GG_OK;
+}
+
 int gg_selftest_wait_timeout(gg_context *ctx, void *stream) {
   if (!ctx) return fail(GG_ERR_ARG, "ctx: null");
   std::lock_guard<std::mutex> lk(ctx->mu);
@@ -1153,7 +1218,9 @@ int gg_reserve(gg_context *ctx, const gg_options *opt, int64_t max_npts,
   j.gcf_dim = max_gcf_dim;
   j.uv_type = GG_C128;
   j.vals_type = vals_type;
-  j.out_type = GG_C128;
+  // complex64 grids of FP32 values need the larger workspace (the lo grid of
+  // the compensated scatter, the merge slots of the moving window)
+  j.out_type = vals_type == GG_C128 ? GG_C128 : GG_C64;
   Plan pl;
   int st = plan_build(ctx, opt, &j, 1, pl);
   if (st) return st;
@@ -1252,7 +1319,9 @@ int gg_grid_batch(gg_context *ctx, const gg_options *opt, const gg_job *jobs,
 }
 
 int gg_read_flags(gg_context *ctx, void *stream, int32_t flags[4]) {
-  if (!ctx || !flags) return fail(GG_ERR_ARG, "null argument");
+  if (!flags) return fail(GG_ERR_ARG, "flags: null");
+  // no context: the flags of the last allocation-free call on this device
+  if (!ctx) return noalloc_read_flags(stream, flags);
   std::lock_guard<std::mutex> lk(ctx->mu);
   GG_CUDA(cudaSetDevice(ctx->device));
   cudaStream_t s = (cudaStream_t)stream;

@@ -15,8 +15,7 @@
 // space and one global tile space; a single job is a batch of one.
 #include <climits>
 
-#include "gg_common.cuh"
-#include "gg_internal.h"
+#include "gg_kernels.cuh"
 
 namespace gg {
 
@@ -364,10 +363,21 @@ cudaError_t run_binning(const BinBuffers &b, cudaStream_t s) {
 
 // ---- work items ---------------------------------------------------------------
 
+// inclusive warp prefix sum
+__device__ __forceinline__ int warp_incl_sum(int v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += y;
+  }
+  return v;
+}
+
 __global__ void __launch_bounds__(256)
     make_items_kernel(const int *bm, const int *tile_base, const int *job_class,
                       int njobs, int total_tiles, ClassChunks chunks, WorkItem *items,
-                      int64_t class_cap, int *counters) {
+                      int64_t class_cap, int *counters, const JobDesc *jobs, ClassSlots slots,
+                      int *heavy_counters, int *flags) {
   const int lane = threadIdx.x & 31;
   for (int base = blockIdx.x * 256 + (threadIdx.x & ~31); base < total_tiles;
        base += gridDim.x * 256) {
@@ -384,16 +394,32 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int c = 0; c < kMaxClasses; ++c) {
       int kc = (cls == c) ? k : 0;
-      int incl = kc;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
+      int incl = warp_incl_sum(kc, lane);
       int tot = __shfl_sync(0xffffffffu, incl, 31);
       int start = 0;
       if (lane == 0 && tot) start = atomicAdd(&counters[c], tot);
       start = __shfl_sync(0xffffffffu, start, 0);
+      // a merge slot for a tile cut into several items (complex64 grids of
+      // classes with slots)
+      const MergeSlots &ms = slots.m[c];
+      int slot = -1;
+      if (ms.base != nullptr) {  // uniform over the warp
+        const int need = kc > 1 && !jobs[j].out_f64 ? 1 : 0;
+        const int hin = warp_incl_sum(need, lane);
+        const int htot = __shfl_sync(0xffffffffu, hin, 31);
+        int h0 = 0;
+        if (lane == 0 && htot) h0 = atomicAdd(&heavy_counters[c], htot);
+        h0 = __shfl_sync(0xffffffffu, h0, 0);
+        if (need) {
+          slot = h0 + hin - 1;
+          if (slot >= ms.cap) {
+            atomicOr(&flags[FLAG_BOUNDS], 1);
+            slot = -1;
+          } else {
+            ms.desc[slot] = make_int2(j, t - tile_base[j]);
+          }
+        }
+      }
       if (kc) {
         WorkItem *dst = items + c * class_cap + start + (incl - kc);
         int local = t - tile_base[j];
@@ -403,6 +429,8 @@ __global__ void __launch_bounds__(256)
           w.bin = local;
           w.start = s0 + i * chunk;
           w.end = min(e0, s0 + (i + 1) * chunk);
+          w.slot = slot;
+          w.pad_[0] = w.pad_[1] = w.pad_[2] = 0;
           dst[i] = w;
         }
       }
@@ -413,11 +441,77 @@ __global__ void __launch_bounds__(256)
 cudaError_t launch_make_items(const int *bookmarks, const int *tile_base,
                               const int *job_class, int njobs, int total_tiles,
                               ClassChunks chunk, WorkItem *items, int64_t class_cap,
-                              int *counters, cudaStream_t s) {
+                              int *counters, cudaStream_t s, const JobDesc *jobs,
+                              const ClassSlots *slots, int *heavy_counters, int *flags) {
   if (total_tiles <= 0) return cudaSuccess;
+  ClassSlots cs{};
+  if (slots && jobs && heavy_counters && flags) cs = *slots;
+  for (int c = 0; c < kMaxClasses; ++c)
+    if (cs.m[c].cap <= 0) cs.m[c].base = nullptr;
   make_items_kernel<<<grid_for(total_tiles), 256, 0, s>>>(
       bookmarks, tile_base, job_class, njobs, total_tiles, chunk, items,
-      class_cap, counters);
+      class_cap, counters, jobs, cs, heavy_counters, flags);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// ---- FP64 merge slots of tiles cut into several work items ---------------------
+
+__global__ void __launch_bounds__(256)
+    merge_zero_kernel(double2 *base, int cells, int cap, const int *count) {
+  const int64_t n = (int64_t)min(*count, cap) * cells;
+  for (int64_t i = blockIdx.x * 256ll + threadIdx.x; i < n; i += (int64_t)gridDim.x * 256)
+    base[i] = make_double2(0.0, 0.0);
+}
+
+cudaError_t launch_merge_zero(const MergeSlots &m, const int *heavy_counter, int sm_count,
+                              cudaStream_t s) {
+  if (!m.base || m.cap <= 0) return cudaSuccess;
+  merge_zero_kernel<<<sm_count * 4, 256, 0, s>>>(m.base, m.cells, m.cap, heavy_counter);
+  count_launch();
+  return cudaGetLastError();
+}
+
+// one CTA per slot (grid-stride over slots): cells of the slot's R x R
+// sub-grid (P planes), origin at the tile's corner minus the halo
+__global__ void __launch_bounds__(256)
+    merge_finalize_kernel(MergeSlots m, const int *count, const JobDesc *jobs, int S, int T,
+                          int P) {
+  const int n = min(*count, m.cap);
+  const int R = T + S - 1, H = S / 2;
+  for (int sl = blockIdx.x; sl < n; sl += gridDim.x) {
+    const int2 d = m.desc[sl];
+    const JobDesc &J = jobs[d.x];
+    const int tile = J.n_gcf > 1 ? d.y / J.n_gcf : d.y;
+    const int ox = (tile % J.ntx) * T - H + 1, oy = (tile / J.ntx) * T - H + 1;
+    const double2 *src = m.base + (size_t)sl * m.cells;
+    for (int i = threadIdx.x; i < P * R * R; i += 256) {
+      const double2 v = src[i];
+      if (v.x == 0.0 && v.y == 0.0) continue;
+      const int p = i / (R * R), c = i - p * R * R;
+      const int gx = ox + c % R, gy = oy + c / R;
+      if ((unsigned)gx < (unsigned)J.N && (unsigned)gy < (unsigned)J.N)
+        out_red(J, (size_t)gy * J.N + gx, p, P, v.x, v.y);
+    }
+  }
+}
+
+cudaError_t launch_merge_finalize(const MergeSlots &m, const int *heavy_counter,
+                                  const JobDesc *jobs, int S, int T, int P, int sm_count,
+                                  cudaStream_t s) {
+  if (!m.base || m.cap <= 0) return cudaSuccess;
+  merge_finalize_kernel<<<sm_count * 8, 256, 0, s>>>(m, heavy_counter, jobs, S, T, P);
+  count_launch();
+  return cudaGetLastError();
+}
+
+__global__ void inject_flags_kernel(int *flags, int bits) {
+  for (int f = 0; f < 4; ++f)
+    if (bits & (1 << f)) atomicOr(&flags[f], 1);
+}
+
+cudaError_t launch_inject_flags(int *flags, int bits, cudaStream_t s) {
+  inject_flags_kernel<<<1, 1, 0, s>>>(flags, bits);
   count_launch();
   return cudaGetLastError();
 }

@@ -86,10 +86,49 @@ constexpr int kMaxClasses = 4;
 struct ClassChunks {
   int c[kMaxClasses];
 };
+// Merge slots per support class (cap 0 or base null: none).  A tile of a job
+// with a complex64 grid that is cut into more than one item gets slot
+// heavy_counters[c]++ of its class: every one of its items carries the slot,
+// and desc[slot] = {job, tile-local bin}.  A slot index beyond the class's
+// cap (the host sizes cap so that this cannot happen) raises FLAG_BOUNDS and
+// leaves the tile on the plain reduction.
+struct ClassSlots {
+  MergeSlots m[kMaxClasses];
+};
 cudaError_t launch_make_items(const int *bookmarks, const int *tile_base,
                               const int *job_class, int njobs, int total_tiles,
                               ClassChunks chunk, WorkItem *items, int64_t class_cap,
-                              int *counters, cudaStream_t s);
+                              int *counters, cudaStream_t s,
+                              const JobDesc *jobs = nullptr, const ClassSlots *slots = nullptr,
+                              int *heavy_counters = nullptr, int *flags = nullptr);
+// Number of merge slots a class needs at most: tiles with more than `chunk`
+// records, at most vis / (chunk + 1) of them.
+inline int merge_slot_cap(int64_t vis, int chunk, int64_t tiles) {
+  int64_t c = vis / ((int64_t)chunk + 1) + 1;
+  if (c > tiles) c = tiles;
+  return (int)c;
+}
+// Clears the slots a class took (heavy_counter on the device) before its
+// window kernel adds into them.
+cudaError_t launch_merge_zero(const MergeSlots &m, const int *heavy_counter, int sm_count,
+                              cudaStream_t s);
+// Rounds every slot of the class once into its job's grid (after the
+// class's window kernel): cell values that are nonzero are reduced into the
+// output with the grid's layout, cells outside the grid skipped.
+cudaError_t launch_merge_finalize(const MergeSlots &m, const int *heavy_counter,
+                                  const JobDesc *jobs, int S, int T, int P, int sm_count,
+                                  cudaStream_t s);
+// ORs `bits` (1 << FLAG_*) into flags[FLAG_*] on the stream: the host-side
+// injection behind gg_debug_inject_device_flags.
+cudaError_t launch_inject_flags(int *flags, int bits, cudaStream_t s);
+// flags of a context (device int32[64], see gg_read_flags)
+int *context_flags(gg_context *c);
+// consumes one pending injection of gg_debug_inject_device_flags: returns
+// its bits (0: none pending)
+int injected_device_flags();
+// gg_read_flags without a context: flags of the last allocation-free call on
+// the current device (gg_noalloc.cu); synchronises the stream
+int noalloc_read_flags(void *stream, int32_t out[4]);
 
 // ---- gridding launches ----------------------------------------------------
 struct GridLaunch {
@@ -116,6 +155,7 @@ struct GridLaunch {
   const int *nitems;
   int *item_next;
   int64_t max_items;
+  MergeSlots merge;        // the class's FP64 merge slots (base null: none)
   // gather: global tiles of the jobs in this launch
   const int *tile_base;    // device [njobs+1]
   int total_tiles;

@@ -24,6 +24,9 @@ struct KParams {
   int T;        // uv tile side, uniform within a launch
   int G;        // oversampling, uniform within a launch
   float sigma;  // GAUSS sigma, uniform within a launch
+  // moving window, compensated FP32 into complex64 grids: FP64 merge slots
+  // of the tiles cut into several work items (base null: none)
+  MergeSlots merge;
 };
 
 // GCF value of tap (a', b') of sub-kernel (sx, sy); KIND 0 table, 1 Gaussian

@@ -13,16 +13,21 @@
 // Limits: at most kNoAllocMaxVis visibilities, img_dim up to 4096 with the
 // default 32-cell tile (kNoAllocMaxTiles uv tiles), one polarisation,
 // complex64 values, a GCF table of at most 65536 taps (G*G*S*S).  The array
-// (about 10 MiB) is held by every GPU that loads this library until the
-// process exits.
+// (kScratchBytes = 12206336 bytes, 11.6 MiB) is held by every GPU that loads
+// this library until the process exits.
 //
 // Set-up: the first call on a device looks up the device address of the
 // array with cudaGetSymbolAddress while that device is current, and caches
 // it; make that first call before any stream capture.  All calls share the
 // array, which keeps whatever the last call left in it: every call clears
-// what must start at zero (histogram, counters, flags, the output grid), and
-// calls that overlap on the GPU (different streams, or different host
-// threads) race on the scratch and corrupt each other's results.
+// what must start at zero (histogram, counters, flags, merge slots, the
+// output grid), and calls that overlap on the GPU (different streams, or
+// different host threads) race on the scratch and corrupt each other's
+// results.  The call's small tables travel as kernel parameters, so nothing
+// on the stream reads host memory and the host never waits.  Device-side
+// failures stay in the array's flag words until the next call:
+// gg_read_flags(NULL, ...) reads them.
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -45,8 +50,11 @@ constexpr size_t kOffBin = kOffJobs + al(sizeof(JobDesc));
 constexpr size_t kOffVisBase = kOffBin + al(sizeof(BinJob));
 constexpr size_t kOffTileBase = kOffVisBase + al(2 * sizeof(int64_t));
 constexpr size_t kOffClass = kOffTileBase + al(2 * sizeof(int));
+// flags [0, 8), item counters [8, 12), item claims [12, 16), merge slots
+// taken [16, 20)
+constexpr int kFlagInts = 32;
 constexpr size_t kOffFlags = kOffClass + al(sizeof(int));
-constexpr size_t kOffPacked = kOffFlags + al(16 * sizeof(int));
+constexpr size_t kOffPacked = kOffFlags + al(kFlagInts * sizeof(int));
 constexpr size_t kOffKey = kOffPacked + al(sizeof(int2) * (kNoAllocMaxVis + 1));
 constexpr size_t kOffBm = kOffKey + al(sizeof(int) * (kNoAllocMaxVis + 1));
 constexpr size_t kOffCursor = kOffBm + al(sizeof(int) * (kNoAllocMaxTiles + 8));
@@ -60,8 +68,19 @@ constexpr size_t kOffItems = kOffSvals + al(sizeof(float2) * (kNoAllocMaxVis + 8
 // row-doubled copy of the GCF table read by the window kernel: up to
 // kNoAllocMaxGcf sub-kernel taps (G*G*S*S), complex64
 constexpr int64_t kNoAllocMaxGcf = 1 << 16;
-constexpr size_t kOffGcf = kOffItems + al(sizeof(WorkItem) * 4 * kClassCap);
-constexpr size_t kScratchBytes = kOffGcf + al(sizeof(float2) * 2 * kNoAllocMaxGcf);
+constexpr size_t kOffGcf = kOffItems + al(sizeof(WorkItem) * kClassCap);  // one class
+// FP64 merge slots of tiles cut into several work items (compensated
+// accumulation into complex64 grids): a fixed area, divided into as many
+// slots of the call's sub-grid size as fit; the records per work item grow
+// when needed so that no more tiles than that are ever cut
+constexpr size_t kMergeBytes = size_t(2) << 20;
+constexpr int kMergeMaxSlots = 1024;
+constexpr size_t kOffMerge = kOffGcf + al(sizeof(float2) * 2 * kNoAllocMaxGcf);
+constexpr size_t kOffMergeDesc = kOffMerge + al(kMergeBytes);
+constexpr size_t kScratchBytes = kOffMergeDesc + al(sizeof(int2) * kMergeMaxSlots);
+
+// the size the header and the documentation state
+static_assert(kScratchBytes == 12206336, "update the stated size of the allocation-free array");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -92,7 +111,40 @@ int ilog2i(int v) {
 
 int noalloc_fail(int code, const char *m) { return set_error(code, m); }
 
+// The call's device tables (job, binning job, bases, class) are kernel
+// parameters written into the scratch by one thread, which also clears the
+// flag and counter words: no host memory is read by the copy engine, so the
+// call does not wait for earlier work on the stream.
+__global__ void noalloc_setup_kernel(JobDesc D, BinJob B, int64_t n, int ntiles, char *ws) {
+  *reinterpret_cast<JobDesc *>(ws + kOffJobs) = D;
+  *reinterpret_cast<BinJob *>(ws + kOffBin) = B;
+  int64_t *vb = reinterpret_cast<int64_t *>(ws + kOffVisBase);
+  vb[0] = 0;
+  vb[1] = n;
+  int *tb = reinterpret_cast<int *>(ws + kOffTileBase);
+  tb[0] = 0;
+  tb[1] = ntiles;
+  *reinterpret_cast<int *>(ws + kOffClass) = 0;
+  int *flags = reinterpret_cast<int *>(ws + kOffFlags);
+  for (int i = 0; i < kFlagInts; ++i) flags[i] = 0;
+}
+
 }  // namespace
+
+// flags of the last allocation-free call on the current device (gg_read_flags
+// with a null context): copied to the host after `stream` completes
+int noalloc_read_flags(void *stream, int32_t out[4]) {
+  char *ws = nullptr;
+  if (int st = setup_scratch(&ws)) return noalloc_fail(st, "noalloc: cudaGetSymbolAddress failed");
+  cudaStream_t s = (cudaStream_t)stream;
+  int32_t h[4];
+  if (cudaMemcpyAsync(h, ws + kOffFlags, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return noalloc_fail(GG_ERR_CUDA, "noalloc: reading the flags failed");
+  for (int i = 0; i < 4; ++i) out[i] = h[i];
+  return GG_OK;
+}
+
 }  // namespace gg
 
 using namespace gg;
@@ -135,6 +187,23 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   if (!job->out || (n > 0 && (!job->uv || !job->vals)) ||
       (opt->gcf_kind == GG_GCF_TABLE && !job->gcf))
     return noalloc_fail(GG_ERR_ARG, "noalloc: null buffer");
+
+  // merge slots (compensated accumulation into a complex64 grid): as many as
+  // the fixed area holds at this sub-grid size; records per item raised so
+  // that fewer tiles than that are cut into several items
+  int chunk = kNoAllocChunk, merge_cap = 0, merge_cells = 0;
+  if (opt->accum == GG_ACC_COMPENSATED && job->out_type == GG_C64) {
+    const int64_t R = T + S - 1;
+    merge_cells = (int)(R * R);
+    const int64_t fit = std::min<int64_t>(kMergeMaxSlots,
+                                          (int64_t)(kMergeBytes / (sizeof(double2) * R * R)));
+    if (fit < 2)
+      return noalloc_fail(GG_ERR_ARG, "noalloc: tile + support too large for the merge area");
+    // a tile of more than `chunk` records takes a slot: at most n/(chunk+1)
+    const int64_t need = (n + fit - 2) / (fit - 1);
+    chunk = (int)std::max<int64_t>(kNoAllocChunk, need);
+    merge_cap = (int)fit;
+  }
 
   char *ws = nullptr;
   int st = setup_scratch(&ws);
@@ -189,23 +258,14 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   B.ntx = (int)ntx;
   B.P = 1;
   B.uv_f64 = D.uv_f64;
-  const int64_t vis_base[2] = {0, n};
-  const int tile_base[2] = {0, (int)(ntx * ntx)};
-  const int cls = 0;
 #define GG_NA(call)                                                        \
   do {                                                                     \
     if ((call) != cudaSuccess) return noalloc_fail(GG_ERR_CUDA, "noalloc: " #call); \
   } while (0)
-  GG_NA(cudaMemcpyAsync(ws + kOffJobs, &D, sizeof D, cudaMemcpyHostToDevice, s));
-  GG_NA(cudaMemcpyAsync(ws + kOffBin, &B, sizeof B, cudaMemcpyHostToDevice, s));
-  GG_NA(cudaMemcpyAsync(ws + kOffVisBase, vis_base, sizeof vis_base, cudaMemcpyHostToDevice, s));
-  GG_NA(cudaMemcpyAsync(ws + kOffTileBase, tile_base, sizeof tile_base,
-                        cudaMemcpyHostToDevice, s));
-  GG_NA(cudaMemcpyAsync(ws + kOffClass, &cls, sizeof cls, cudaMemcpyHostToDevice, s));
-  // pageable-source copies above complete before returning to the host, so
-  // the stack tables may go out of scope
+  noalloc_setup_kernel<<<1, 1, 0, s>>>(D, B, n, (int)(ntx * ntx), ws);
+  count_launch();
+  GG_NA(cudaGetLastError());
   int *flags = (int *)(ws + kOffFlags);
-  GG_NA(cudaMemsetAsync(flags, 0, 16 * sizeof(int), s));
   const size_t out_bytes = (size_t)(D.out_f64 ? 16 : 8) * N * N;
   GG_NA(cudaMemsetAsync(job->out, 0, out_bytes, s));
 
@@ -237,9 +297,18 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   GG_NA(run_binning(b, s));
 
   WorkItem *items = (WorkItem *)(ws + kOffItems);
-  const ClassChunks chunks = {{kNoAllocChunk, kNoAllocChunk, kNoAllocChunk, kNoAllocChunk}};
+  ClassChunks chunks = {{chunk, chunk, chunk, chunk}};
+  ClassSlots slots{};
+  if (merge_cap > 0) {
+    slots.m[0].base = (double2 *)(ws + kOffMerge);
+    slots.m[0].desc = (int2 *)(ws + kOffMergeDesc);
+    slots.m[0].cap = merge_cap;
+    slots.m[0].cells = merge_cells;
+  }
   GG_NA(launch_make_items(b.bookmarks, b.tile_base, (const int *)(ws + kOffClass), 1,
-                          b.total_tiles, chunks, items, kClassCap, flags + 8, s));
+                          b.total_tiles, chunks, items, kClassCap, flags + 8, s,
+                          (const JobDesc *)(ws + kOffJobs), &slots, flags + 16, flags));
+  GG_NA(launch_merge_zero(slots.m[0], flags + 16, sms, s));
   GridLaunch g{};
   g.jobs = (const JobDesc *)(ws + kOffJobs);
   g.njobs = 1;
@@ -258,7 +327,11 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   g.nitems = flags + 8;
   g.item_next = flags + 12;
   g.max_items = kClassCap;
+  g.merge = slots.m[0];
   GG_NA(launch_window(g, s));
+  GG_NA(launch_merge_finalize(slots.m[0], flags + 16, (const JobDesc *)(ws + kOffJobs), (int)S, T,
+                              1, sms, s));
+  if (const int bits = injected_device_flags()) GG_NA(launch_inject_flags(flags, bits, s));
 #undef GG_NA
   return GG_OK;
 }

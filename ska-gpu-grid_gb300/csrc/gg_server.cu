@@ -46,6 +46,7 @@ struct Req {
   double t_arrival = 0, t_launch = 0, t_done = 0;
   int state = R_SCHEDULED;
   int status = GG_OK;
+  int device_flags = 0;       // GG_DEVFLAG_* of its batch
   int64_t bytes = 0;          // budget charged while admitted
   int64_t resident_bytes = 0; // part of `bytes` kept until release
   void *d_uv = nullptr, *d_vals = nullptr, *d_out = nullptr;
@@ -56,6 +57,9 @@ struct Req {
 struct Slot {
   cudaStream_t s = nullptr;
   gg_context *ctx = nullptr;
+  // pinned copy of the batch's device flag words, read back behind the
+  // batch's kernels and checked when the batch completes
+  int32_t *hflags = nullptr;
   std::vector<Req *> batch;
   bool busy = false;
   bool done = false;
@@ -121,7 +125,15 @@ int64_t estimate(const gg_server *srv, const gg_request &r) {
   const int64_t inputs =
       (r.flags & GG_REQ_INPUTS_ON_DEVICE) ? 0 : n * (elem(r.uv_type) + elem(r.vals_type) * P);
   const int64_t tiles = ((N + 15) / 16) * ((N + 15) / 16);
-  const int64_t ws = n * (8 + 4 + 8 + 4 + elem(r.vals_type) * P) + tiles * 16;
+  int64_t ws = n * (8 + 4 + 8 + 4 + elem(r.vals_type) * P) + tiles * 16;
+  // FP64 merge slots of tiles cut into several work items (compensated FP32
+  // into a complex64 grid): at most one per 1025 records, each a sub-grid of
+  // side T + S - 1 with tiles of up to 32 cells
+  const gg_options &o = srv->cfg.options;
+  if (o.accum == GG_ACC_COMPENSATED && r.vals_type == GG_C64 && r.out_type == GG_C64) {
+    const int64_t R = 32 + r.gcf_dim - 1;
+    ws += (n / 1025 + 1) * (R * R * 16 * P + 8);
+  }
   return grid + inputs + ws + 4096;
 }
 
@@ -152,7 +164,28 @@ int validate(const gg_server *srv, const gg_request &r) {
 
 void finish_batch(gg_server *srv, Slot *slot) {
   const double t = srv->now();
+  // device flags of the batch: a timeout, unsorted input or a failed bounds
+  // check fails every request of the batch (its grids are incomplete);
+  // dropped visibilities are reported and the requests succeed
+  const int32_t *h = slot->hflags;
+  const int bits = (h[gg::FLAG_INDEX] ? GG_DEVFLAG_INDEX : 0) |
+                   (h[gg::FLAG_TIMEOUT] ? GG_DEVFLAG_TIMEOUT : 0) |
+                   (h[gg::FLAG_UNSORTED] ? GG_DEVFLAG_UNSORTED : 0) |
+                   (h[gg::FLAG_BOUNDS] ? GG_DEVFLAG_BOUNDS : 0);
+  const int dev_status = h[gg::FLAG_TIMEOUT]    ? GG_ERR_TIMEOUT
+                         : h[gg::FLAG_UNSORTED] ? GG_ERR_UNSORTED
+                         : h[gg::FLAG_BOUNDS]   ? GG_ERR_STATE
+                                                : GG_OK;
   for (Req *q : slot->batch) {
+    q->device_flags = bits;
+    if (q->state == R_LAUNCHED && q->status == GG_OK && dev_status != GG_OK) {
+      q->status = dev_status;
+      if (q->own_out && q->d_out) {  // a resident grid of a failed request
+        cudaFreeAsync(q->d_out, slot->s);
+        q->own_out = false;
+        q->d_out = nullptr;
+      }
+    }
     if (q->state == R_LAUNCHED && q->status == GG_OK) {
       q->state = R_DONE;
       q->t_done = t;
@@ -239,7 +272,19 @@ void launch_batch(gg_server *srv, Slot *slot) {
   // server is young; afterwards the cached choices are reused
   gg_options opt = srv->cfg.options;
   if (opt.autotune == 1 && slot->seq >= GG_SERVER_TUNE_BATCHES) opt.autotune = 2;
+  int *dflags = gg::context_flags(slot->ctx);
+  for (int i = 0; i < 4; ++i) slot->hflags[i] = 0;
+  if (st == GG_OK && cudaMemsetAsync(dflags, 0, 4 * sizeof(int), s) != cudaSuccess)
+    st = GG_ERR_CUDA;
   if (st == GG_OK) st = gg_grid_batch(slot->ctx, &opt, jobs.data(), (int32_t)jobs.size(), s);
+  if (st == GG_OK) {
+    if (const int inj = gg::injected_device_flags())
+      if (gg::launch_inject_flags(dflags, inj, s) != cudaSuccess) st = GG_ERR_CUDA;
+  }
+  if (st == GG_OK &&
+      cudaMemcpyAsync(slot->hflags, dflags, 4 * sizeof(int), cudaMemcpyDeviceToHost, s) !=
+          cudaSuccess)
+    st = GG_ERR_CUDA;
   for (Req *q : slot->batch) {
     if (st != GG_OK && q->status == GG_OK) q->status = st;
     const gg_request &r = q->r;
@@ -369,10 +414,22 @@ int gg_server_create(gg_server **out, const gg_server_config *cfg) {
       for (auto &x : srv->slots) {
         gg_destroy(x->ctx);
         cudaStreamDestroy(x->s);
+        cudaFreeHost(x->hflags);
       }
       return st;
     }
     cudaStreamCreateWithFlags(&sl->s, cudaStreamNonBlocking);
+    if (cudaMallocHost(&sl->hflags, 4 * sizeof(int32_t)) != cudaSuccess) {
+      gg_destroy(sl->ctx);
+      cudaStreamDestroy(sl->s);
+      for (auto &x : srv->slots) {
+        gg_destroy(x->ctx);
+        cudaStreamDestroy(x->s);
+        cudaFreeHost(x->hflags);
+      }
+      return set_error(GG_ERR_NOMEM, "server: pinned flag words");
+    }
+    for (int i = 0; i < 4; ++i) sl->hflags[i] = 0;
     srv->slots.push_back(std::move(sl));
   }
   gg_server *p = srv.release();
@@ -509,6 +566,7 @@ int gg_server_wait(gg_server *srv, int64_t ticket, double timeout_s, gg_result *
   if (res) {
     memset(res, 0, sizeof *res);
     res->status = q->state == R_CANCELLED ? GG_ERR_CANCELLED : q->status;
+    res->device_flags = q->device_flags;
     res->latency_s = q->t_done - q->t_arrival;
     res->queue_s = q->t_launch > 0 ? q->t_launch - q->t_arrival : 0.0;
     res->device_out = (q->r.flags & GG_REQ_KEEP_RESIDENT) ? q->d_out : nullptr;
@@ -637,6 +695,7 @@ int gg_server_destroy(gg_server *srv) {
   for (auto &sl : srv->slots) {
     gg_destroy(sl->ctx);
     cudaStreamDestroy(sl->s);
+    cudaFreeHost(sl->hflags);
   }
   for (void *p : srv->gcf_ptr) cudaFree(p);
   delete srv;

@@ -41,12 +41,33 @@ struct JobDesc {
 };
 
 // A slice of one uv tile's sorted visibilities: the unit of the device work
-// queue of the moving-window kernel (and of batched launches).
-struct WorkItem {
+// queue of the moving-window kernel (and of batched launches).  `slot` is the
+// FP64 merge slot of the tile (see MergeSlots) when the tile is cut into
+// several items and its partial sub-grids must be merged without FP32
+// roundings; -1 otherwise.
+struct __align__(16) WorkItem {
   int job;
   int bin;
   int start;
   int end;
+  int slot;
+  int pad_[3];
+};
+
+// FP64 merge slots of one support class of a compensated moving-window
+// launch.  A tile cut into k > 1 work items would otherwise send k partial
+// sub-grids to its FP32 output cells, each reduction rounding once (an error
+// growing with k).  Instead every item of such a tile adds its partial
+// sub-grid exactly (hi + lo in FP64) into the tile's slot: `cells` = P * R^2
+// double2 values, R = T + S - 1 the sub-grid side; a finalize kernel then
+// rounds every slot cell once into the grid.  Only for FP32 values with
+// compensated accumulation into complex64 grids (complex128 grids take the
+// FP64 reduction directly).
+struct MergeSlots {
+  double2 *base;  // [cap][cells], null: no slots in this class
+  int2 *desc;     // [cap]: {job, bin} of the tile owning each slot
+  int cap;        // slots available
+  int cells;      // double2 values per slot
 };
 
 template <typename T> struct vec2_of;

@@ -190,6 +190,15 @@ __device__ __forceinline__ void out_cell(const JobDesc &J, size_t cell, int p,
   out_red(J, cell, p, P, c.x, c.y);
 }
 
+// exact (hi + lo in FP64) addition of a compensated sub-grid cell into a merge
+// slot cell; the other cell types never reach a slot
+__device__ __forceinline__ void merge_cell(double2 *d, const float4 &c) {
+  red_add(&d->x, (double)c.x + (double)c.z);
+  red_add(&d->y, (double)c.y + (double)c.w);
+}
+__device__ __forceinline__ void merge_cell(double2 *, const float2 &) {}
+__device__ __forceinline__ void merge_cell(double2 *, const double2 &) {}
+
 // ---- configuration ----------------------------------------------------------------
 constexpr int kWinThreads = 256;
 // longest register run (records) of the compensated mode: a run of L terms
@@ -347,7 +356,12 @@ __global__ void __launch_bounds__(kWinThreads, win_min_ctas(S, W, MODE))
     const int ox = tx * T - H + 1, oy = ty * T - H + 1;  // sub-grid origin
     const int n = w.end - w.start;
     const int nch = (n + K - 1) / K;
-    const bool direct = (long long)n * S * S < (long long)R * R;
+    // FP64 merge slot of a tile cut into several items (compensated FP32 into
+    // a complex64 grid): the item's sub-grid is added into it exactly
+    double2 *const mslot = MODE == 1 && kp.merge.base && w.slot >= 0
+                               ? kp.merge.base + (size_t)w.slot * kp.merge.cells + (size_t)p * R * R
+                               : nullptr;
+    const bool direct = !mslot && (long long)n * S * S < (long long)R * R;
     // what follows in the stream: the next plane of this item, or the next item
     const int nxt_item = p + 1 < P ? item : next;
     const int nxt_p = p + 1 < P ? p + 1 : 0;
@@ -657,9 +671,13 @@ __global__ void __launch_bounds__(kWinThreads, win_min_ctas(S, W, MODE))
         const CellT cv = region[i];
         if (cell_nonzero(cv)) {
           region[i] = CellT{};
-          const int gx = ox + cx, gy = oy + cy;
-          if ((unsigned)gx < (unsigned)N && (unsigned)gy < (unsigned)N)
-            out_cell(J, (size_t)gy * N + gx, p, P, cv);
+          if (mslot) {
+            merge_cell(mslot + i, cv);
+          } else {
+            const int gx = ox + cx, gy = oy + cy;
+            if ((unsigned)gx < (unsigned)N && (unsigned)gy < (unsigned)N)
+              out_cell(J, (size_t)gy * N + gx, p, P, cv);
+          }
         }
         cx += sdx;
         cy += sdy;
@@ -831,6 +849,7 @@ cudaError_t launch_window(const GridLaunch &g, cudaStream_t s) {
   kp.T = g.tile;
   kp.G = g.G;
   kp.sigma = g.sigma;
+  kp.merge = g.accum == GG_ACC_COMPENSATED && !g.vals_f64 ? g.merge : MergeSlots{};
   const int w = win_warps(g.S, g.group_warps, g.tile);
   switch (g.S) {
     case 4: return win_modes<4, 1>(g, kp, s);

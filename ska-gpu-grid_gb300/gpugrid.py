@@ -35,6 +35,7 @@ MODE_SCATTER, MODE_GATHER, MODE_WINDOW, MODE_AUTO = range(4)
 LAYOUT_INTERLEAVED, LAYOUT_PLANAR, LAYOUT_REFERENCE = range(3)
 ACC_PLAIN, ACC_COMPENSATED = range(2)
 GCF_TABLE, GCF_GAUSSIAN, GCF_COUNT, GCF_WPHASE = range(4)
+DEVFLAG_INDEX, DEVFLAG_TIMEOUT, DEVFLAG_UNSORTED, DEVFLAG_BOUNDS = 1, 2, 4, 8
 
 MODES = {"scatter": MODE_SCATTER, "gather": MODE_GATHER,
          "window": MODE_WINDOW, "auto": MODE_AUTO}
@@ -93,7 +94,7 @@ class gg_request(ctypes.Structure):
 
 
 class gg_result(ctypes.Structure):
-    _fields_ = [("status", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+    _fields_ = [("status", ctypes.c_int32), ("device_flags", ctypes.c_int32),
                 ("latency_s", ctypes.c_double), ("queue_s", ctypes.c_double),
                 ("device_out", ctypes.c_void_p)]
 
@@ -162,6 +163,8 @@ def _load():
         "gg_autotune_clear": ([], ctypes.c_int),
         "gg_selftest_wait_timeout": ([vp, vp], ctypes.c_int),
         "gg_debug_inject_alloc_failures": ([i32], ctypes.c_int),
+        "gg_debug_inject_device_flags": ([i32, i32], ctypes.c_int),
+        "gg_grid_device_noalloc": ([P(gg_options), P(gg_job), vp], ctypes.c_int),
         "gg_autotune_report": ([ctypes.c_char_p, sz], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
@@ -513,9 +516,13 @@ class Server:
             tickets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
         return tickets
 
-    def wait(self, ticket: int, timeout: float = -1.0) -> gg_result:
+    def wait(self, ticket: int, timeout: float = -1.0, check: bool = True) -> gg_result:
+        """The request's result; a failed request raises GridError unless
+        ``check`` is false (then its ``status`` and ``device_flags`` tell)."""
         r = gg_result()
-        _check(LIB.gg_server_wait(self._h, ticket, timeout, ctypes.byref(r)))
+        st = LIB.gg_server_wait(self._h, ticket, timeout, ctypes.byref(r))
+        if check or st == ERR_TIMEOUT and r.status == OK:
+            _check(st)
         return r
 
     def release(self, ticket: int) -> None:
@@ -559,6 +566,32 @@ def autotune_report() -> str:
 
 def autotune_clear() -> None:
     _check(LIB.gg_autotune_clear())
+
+
+def inject_device_flags(bits: int, count: int = 1) -> None:
+    """Test hook: the next ``count`` served batches / allocation-free calls get
+    the GG_DEVFLAG_* ``bits`` raised in their device flag word (by a host-side
+    kernel launch behind their gridding, before the flags are read back)."""
+    _check(LIB.gg_debug_inject_device_flags(bits, count))
+
+
+def grid_device_noalloc(opts: Options, job: gg_job, stream=None) -> None:
+    """gg_grid_device_noalloc: moving-window gridding with the library's fixed
+    scratch array (no allocation); asynchronous on the torch stream."""
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    _check(LIB.gg_grid_device_noalloc(ctypes.byref(opts.c()), ctypes.byref(job),
+                                      ctypes.c_void_p(s.cuda_stream)))
+
+
+def noalloc_flags(stream=None) -> list[int]:
+    """flag counters of the last allocation-free call on the current device
+    (gg_read_flags with a null context; synchronises the stream)"""
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    f = (ctypes.c_int32 * 4)()
+    _check(LIB.gg_read_flags(None, ctypes.c_void_p(s.cuda_stream), f))
+    return list(f)
 
 
 def kernel_launches() -> int:

@@ -30,6 +30,25 @@ def rel_err(a, ref):
     return float(np.abs(a - ref).max() / (den if den > 0 else 1.0))
 
 
+def cell_err(a, ref, mag):
+    """Per-cell forward error of a planar grid a (2, P, N, N) against the
+    oracle ref: |a - ref| (complex modulus) / mag at every cell, mag the
+    oracle's sum of |val| * |w| over that cell's additions (O.grid_mag,
+    shape (P, N, N)).  Returns (max, rms) over the cells with mag > 0; a
+    nonzero value at a cell with mag == 0 counts as an infinite error."""
+    a = np.asarray(a, np.float64)
+    ref = np.asarray(ref, np.float64)
+    mag = np.asarray(mag, np.float64).reshape(a.shape[1:])
+    d = np.hypot(a[0] - ref[0], a[1] - ref[1])
+    hit = mag > 0
+    if np.any(d[~hit] != 0):
+        return float("inf"), float("inf")
+    if not hit.any():
+        return 0.0, 0.0
+    e = d[hit] / mag[hit]
+    return float(e.max()), float(np.sqrt((e * e).mean()))
+
+
 def rms_rel_err(a, ref):
     a = np.asarray(a, np.float64)
     ref = np.asarray(ref, np.float64)

@@ -197,3 +197,20 @@ def test_header_constants_match_python_mirror():
     assert int(consts["GG_SERVER_TUNE_BATCHES"]) == gg.SERVER_TUNE_BATCHES
     assert int(consts["GG_REQ_KEEP_RESIDENT"]) == gg.REQ_KEEP_RESIDENT
     assert int(consts["GG_GCF_WPHASE"]) == gg.GCF_WPHASE
+
+
+def test_noalloc_array_size_as_documented():
+    """The size of the allocation-free entry point's fixed array stated in
+    include/gg.h is the size of the array in libgg.so (symbol table)."""
+    import shutil
+    import subprocess
+    nm = shutil.which("nm")
+    if not nm:
+        pytest.skip("no nm")
+    hdr = open(os.path.join(ROOT, "include", "gg.h")).read()
+    m = re.search(r"array \((\d+) bytes", hdr)
+    assert m, "gg.h states the array size in bytes"
+    out = subprocess.run([nm, "-S", "-C", gg.LIB_PATH], capture_output=True, text=True).stdout
+    sizes = [int(line.split()[1], 16) for line in out.splitlines()
+             if "g_noalloc_scratch" in line and len(line.split()) >= 4]
+    assert sizes == [int(m.group(1))], sizes

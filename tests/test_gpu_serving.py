@@ -236,3 +236,59 @@ def test_autotune_lookup_only_never_times(ctx):
     got = grid_alone(ctx, o, N, S, uv, vals, GCF[S])
     assert gg.autotune_report().strip() == ""
     assert relerr(got, grid_alone(ctx, OPTS, N, S, uv, vals, GCF[S])) <= TOL
+
+
+def test_server_reports_device_flags(ctx):
+    """Device-side failures reach the requests of their batch: the server
+    reads the batch's flag words back behind its kernels.  A bounded-wait
+    timeout (raised from the host by a one-thread kernel, no real wait) fails
+    the batch's requests with GG_ERR_TIMEOUT; dropped visibilities are
+    reported and the request succeeds; input declared tile-sorted that is
+    not (a real device detection) fails with GG_ERR_UNSORTED.  Requests of
+    later batches are unaffected."""
+    rng = np.random.default_rng(6)
+    data = [make_request_data(600 + k, rng) for k in range(3)]
+    with gg.Server(streams=1, options=OPTS) as srv:
+        gids = {S: srv.add_gcf(GCF[S]) for S in (8, 16)}
+
+        def one(k, inject=0, check=True):
+            N, S, uv, vals = data[k]
+            out = np.full(N * N, np.nan, np.complex64)
+            gg.inject_device_flags(inject, 1 if inject else 0)
+            try:
+                t = srv.submit(gg.Server.request(uv.ctypes.data, vals.ctypes.data,
+                                                 out.ctypes.data, len(uv), N, S, gids[S]))
+                r = srv.wait(t, timeout=60, check=check)
+            finally:
+                gg.inject_device_flags(0, 0)
+            srv.release(t)
+            return r, out
+
+        r, _ = one(0, gg.DEVFLAG_TIMEOUT, check=False)
+        assert r.status == gg.ERR_TIMEOUT and r.device_flags == gg.DEVFLAG_TIMEOUT
+        r, out = one(1, gg.DEVFLAG_INDEX)
+        assert r.status == gg.OK and r.device_flags == gg.DEVFLAG_INDEX
+        N, S, uv, vals = data[1]
+        assert relerr(out, grid_alone(ctx, OPTS, N, S, uv, vals, GCF[S])) <= TOL
+        r, out = one(2)
+        assert r.status == gg.OK and r.device_flags == 0
+        st = srv.stats()
+        assert st["completed"] == 2 and st["failed"] == 1 and st["hbm_in_use"] == 0
+    srt = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
+                     layout=gg.LAYOUT_INTERLEAVED, input_sorted=True)
+    with gg.Server(streams=1, options=srt) as srv:
+        N, S = 256, 8
+        uv, vals = synth.uniform(5000, 8, N - 8, seed=61)   # not tile-sorted
+        gid = srv.add_gcf(GCF[S])
+        out = np.zeros(N * N, np.complex64)
+        t = srv.submit(gg.Server.request(uv.ctypes.data, vals.ctypes.data, out.ctypes.data,
+                                         len(uv), N, S, gid))
+        r = srv.wait(t, timeout=60, check=False)
+        assert r.status == gg.ERR_UNSORTED and r.device_flags & gg.DEVFLAG_UNSORTED
+        srv.release(t)
+        order = synth.tile_sort(uv, N, 32, S)
+        uv2, v2 = np.ascontiguousarray(uv[order]), np.ascontiguousarray(vals[order])
+        t = srv.submit(gg.Server.request(uv2.ctypes.data, v2.ctypes.data, out.ctypes.data,
+                                         len(uv2), N, S, gid))
+        assert srv.wait(t, timeout=60).device_flags == 0
+        srv.release(t)

@@ -202,3 +202,53 @@ def test_degrid_oracle_drops_out_of_range_indices_and_is_thread_independent():
     # a visibility far off the grid touches no cell
     far = synth.fr(np.array([[-40.0, 10.0], [10.0, N + 40.0]]))
     assert np.all(O.degrid_pz(far, g, gcf, N, S) == 0)
+
+
+def _pairs(c):
+    c = np.asarray(c).reshape(-1)
+    return np.stack([c.real, c.imag], -1).astype(np.float64)
+
+
+@pytest.mark.parametrize("n_gcf", [1, 3])
+def test_magnitude_grid_bounds_every_cell(n_gcf):
+    """The per-cell magnitude sum (denominator of the per-cell error) covers
+    exactly the additions of the gridder: |grid| <= mag at every cell, mag is
+    zero exactly where no tap lands, it equals the grid for positive real
+    values and tables, and it does not depend on the thread count."""
+    N, S, P = 96, 8, 2
+    rng = np.random.default_rng(41)
+    uv, _ = synth.uniform(3000, -S, N + S, seed=41)
+    vals = (rng.standard_normal(len(uv) * P) + 1j * rng.standard_normal(len(uv) * P))
+    tabs = np.concatenate([
+        (synth.gcf_table(synth.gaussian_gcf_1d(S, sigma=2 + t)) * np.exp(0.7j * t)).reshape(-1)
+        for t in range(n_gcf)])
+    idx = rng.integers(0, n_gcf, len(uv)).astype(np.int32)
+    grid = O.grid_pz_gcfinx(uv, _pairs(vals), idx, _pairs(tabs), N, S, pols=P)
+    mag = O.grid_mag(uv, _pairs(vals), tabs, N, S, pols=P, gcfinx=idx)
+    assert mag.shape == (P, N, N)
+    assert np.all(np.hypot(grid[0], grid[1]) <= mag * (1 + 1e-12))
+    ones = O.grid_pz_gcfinx(uv, np.ones((len(uv) * P, 2)) * [1, 0], idx, np.abs(_pairs(tabs)),
+                            N, S, pols=P)
+    assert np.array_equal(mag > 0, ones[0] > 0)
+    assert np.array_equal(mag, O.grid_mag(uv, _pairs(vals), tabs, N, S, pols=P, gcfinx=idx,
+                                          nthreads=7))
+    pos = np.abs(vals).astype(np.complex128)
+    absg = np.abs(tabs).astype(np.complex128)
+    g2 = O.grid_pz_gcfinx(uv, _pairs(pos), idx, _pairs(absg), N, S, pols=P)
+    m2 = O.grid_mag(uv, _pairs(pos), absg, N, S, pols=P, gcfinx=idx)
+    assert np.allclose(g2[0], m2, rtol=1e-14, atol=0) and not g2[1].any()
+
+
+def test_cell_error_metric():
+    """cell_err: |a - ref| / mag per cell; an error where nothing was gridded
+    is infinite; cells with mag 0 and no error are left out."""
+    from helpers import cell_err
+    ref = np.zeros((2, 1, 4, 4))
+    mag = np.zeros((1, 4, 4))
+    ref[0, 0, 1, 1], mag[0, 1, 1] = 1.0, 2.0
+    a = ref.copy()
+    a[1, 0, 1, 1] = 1e-3
+    mx, rms = cell_err(a, ref, mag)
+    assert mx == pytest.approx(5e-4) and rms == pytest.approx(5e-4)
+    a[0, 0, 0, 0] = 1e-30
+    assert cell_err(a, ref, mag)[0] == float("inf")
