@@ -87,7 +87,7 @@ WORKLOADS = {
               "FP64 scatter")),
     "disk8192": dict(
         kind="single", N=8192, S=32, npts=1 << 24, gen="disk", vals="c64", out="c128",
-        mode="auto", accum="comp", gcf="gauss", precision_study=True,
+        mode="auto", accum="comp", gcf="gauss", precision_study=True, check_window=1024,
         desc=("8192^2 grid (complex128 output of FP32 compensated "
               "accumulation); 2^24 visibilities, uniform disk; N(0,1) values "
               "with 1% outliers at 1e3; support 32, oversample 8; GCF computed "
@@ -278,9 +278,40 @@ def roofline(kernel, alg_bytes, kern_ms, tag, taps=None, dev=0):
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle restatement of gridCPU_pz on the host cores
 # ---------------------------------------------------------------------------
-def cpu_rate(jobs, budget_s, threads=None):
-    """jobs: list of (uv, vals, gcf, N, S).  Grids jobs until about budget_s
-    seconds have been spent; returns (Mvis/s, visibilities, seconds)."""
+# The CPU sample of a workload -- the same in the line's cpu_baseline and in
+# the reference arm (--impl reference): for the request stream and the batch,
+# the first whole jobs up to CPU_SAMPLE_VIS visibilities; for a single job, a
+# prefix of its visibilities (smaller for support 32, whose taps cost 4x).
+CPU_SAMPLE_VIS = 3_500_000
+
+
+def stream_seed(kind, rank=0):
+    return (7 if kind == "served" else 17) + rank
+
+
+def cpu_sample(w, rank=0):
+    """(jobs [(uv, vals, gcf, N, S)], description) of the workload's CPU sample"""
+    if w["kind"] == "single":
+        uv, vals, gcf = make_single(w, seed=1000 + rank)
+        m = min(len(uv), (1 << 18) if w["S"] >= 32 else (1 << 20))
+        return ([(uv[:m], vals[:m], gcf, w["N"], w["S"])],
+                f"the first {m} visibilities of the workload")
+    pools, specs, gcfs = stream_inputs(w["n"], seed=stream_seed(w["kind"], rank))
+    jobs, vis = [], 0
+    for i in range(w["n"]):
+        uv, vals = slice_of(pools, specs, i)
+        if jobs and vis + len(uv) > CPU_SAMPLE_VIS:
+            break
+        jobs.append((uv, vals, gcfs[int(specs["S"][i])], int(specs["side"][i]),
+                     int(specs["S"][i])))
+        vis += len(uv)
+    return jobs, f"the first {len(jobs)} jobs of the stream ({vis} visibilities)"
+
+
+def cpu_rate(jobs, threads=None):
+    """Grids the sample once on the host cores (the oracle restatement of
+    gridCPU_pz over all threads in row bands); returns (Mvis/s,
+    visibilities, seconds, threads)."""
     import oracle as O
     threads = threads or os.cpu_count() or 1
     vis, spent = 0, 0.0
@@ -289,9 +320,15 @@ def cpu_rate(jobs, budget_s, threads=None):
         O.grid_pz(uv, pairs(vals), pairs(gcf), N, S, nthreads=threads)
         spent += time.perf_counter() - t0
         vis += len(uv)
-        if spent >= budget_s:
-            break
     return vis / spent / 1e6, vis, spent, threads
+
+
+def cpu_baseline(w, rank=0):
+    jobs, desc = cpu_sample(w, rank)
+    v, n, t, c = cpu_rate(jobs)
+    return {"value": round(v, 4), "unit": "Mvis/s", "cores": c, "kind": "port",
+            "sample": f"{desc}, {t:.2f} s; gridCPU_pz restatement (oracle/grid_oracle.c) "
+                      f"over {c} row bands, bit-identical to the single-threaded reference"}
 
 
 # ---------------------------------------------------------------------------
@@ -326,20 +363,77 @@ class DevicePools:
         return (uv.data_ptr() + (s * L + off) * 16, v.data_ptr() + (s * L + off) * 8)
 
 
-def check_sample(grids, pools, specs, gcfs, idx):
-    """max / RMS relative error of device grids vs the FP64 oracle"""
+ACC_NOTE = ("max_rel / rms_rel: normwise, |gpu - oracle| / max |oracle| (max) and "
+            "||gpu - oracle|| / ||oracle|| (rms) over the grid; cell_max / cell_rms: per "
+            "cell, |gpu - oracle| / sum |v||w| of the cell's additions (forward error of "
+            "each cell's sum), over the cells that receive any")
+
+
+class ErrAcc:
+    """normwise and per-cell error of grids against the FP64 oracle,
+    accumulated over several grids (planar (2, P, N, N) float64 each)"""
+
+    def __init__(self):
+        self.worst = self.num = self.den = 0.0
+        self.cmax = self.csq = 0.0
+        self.cells = 0
+
+    def add(self, got, ref, mag):
+        self.worst = max(self.worst, float(np.abs(got - ref).max() /
+                                           max(np.abs(ref).max(), 1e-300)))
+        self.num += float(((got - ref) ** 2).sum())
+        self.den += float((ref ** 2).sum())
+        d = np.hypot(got[0] - ref[0], got[1] - ref[1])
+        hit = mag > 0
+        if np.any(d[~hit] != 0):
+            self.cmax = float("inf")
+        e = d[hit] / mag[hit]
+        if e.size:
+            self.cmax = max(self.cmax, float(e.max()))
+            self.csq += float((e * e).sum())
+            self.cells += int(e.size)
+
+    def result(self, **extra):
+        r = {"max_rel": self.worst, "rms_rel": (self.num / max(self.den, 1e-300)) ** 0.5,
+             "cell_max": self.cmax,
+             "cell_rms": (self.csq / max(self.cells, 1)) ** 0.5}
+        r.update(extra)
+        r["reference"] = "FP64 oracle (gridCPU_pz restatement)"
+        return r
+
+
+def oracle_pair(uv, vals, gcf, N, S):
+    """(planar FP64 grid, per-cell magnitude sums) of the oracle"""
     import oracle as O
-    worst, rms_num, rms_den = 0.0, 0.0, 0.0
+    t = os.cpu_count() or 1
+    return (O.grid_pz(uv, pairs(vals), pairs(gcf), N, S, nthreads=t),
+            O.grid_mag(uv, pairs(vals), pairs(gcf), N, S, nthreads=t))
+
+
+def window_reference(uv, vals, gcf, N, S, x0, y0, B):
+    """Oracle of the B x B window [x0, x0+B) x [y0, y0+B) of an N^2 grid:
+    every visibility whose footprint can reach the window, shifted by an
+    integer offset (exact in FP64 and keeping u, v float-representable, so
+    main and oversample indices shift exactly) onto a (B + 2S)^2 grid.
+    Returns (ref, mag) of the window, planar (2, 1, B, B) and (1, B, B)."""
+    m = np.floor(uv)
+    keep = ((m[:, 0] >= x0 - S) & (m[:, 0] < x0 + B + S) &
+            (m[:, 1] >= y0 - S) & (m[:, 1] < y0 + B + S))
+    sub = uv[keep] - np.array([x0 - S, y0 - S], np.float64)
+    ref, mag = oracle_pair(sub, vals[keep], gcf, B + 2 * S, S)
+    return ref[:, :, S:S + B, S:S + B], mag[:, S:S + B, S:S + B], int(keep.sum())
+
+
+def check_sample(grids, pools, specs, gcfs, idx):
+    """normwise and per-cell error of device grids vs the FP64 oracle"""
+    acc = ErrAcc()
     for i, g in zip(idx, grids):
         uv, vals = slice_of(pools, specs, i)
         N, S = int(specs["side"][i]), int(specs["S"][i])
-        ref = O.grid_pz(uv, pairs(vals), pairs(gcfs[S]), N, S, nthreads=os.cpu_count())
+        ref, mag = oracle_pair(uv, vals, gcfs[S], N, S)
         got = np.stack([g.real, g.imag]).reshape(2, 1, N, N).astype(np.float64)
-        worst = max(worst, float(np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300)))
-        rms_num += float(((got - ref) ** 2).sum())
-        rms_den += float((ref ** 2).sum())
-    return {"max_rel": worst, "rms_rel": (rms_num / max(rms_den, 1e-300)) ** 0.5,
-            "jobs_checked": len(idx), "reference": "FP64 oracle (gridCPU_pz restatement)"}
+        acc.add(got, ref, mag)
+    return acc.result(jobs_checked=len(idx), metrics=ACC_NOTE)
 
 
 def cudart():
@@ -359,7 +453,7 @@ def run_served(args, rank, world, local_rank, dist):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     n = w["n"]
-    pools, specs, gcfs = stream_inputs(n, seed=7 + rank)
+    pools, specs, gcfs = stream_inputs(n, seed=stream_seed("served", rank))
     total_vis = int(specs["nvis"].sum())
     dp = DevicePools(pools, dev)
     opts = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
@@ -574,12 +668,6 @@ def run_served(args, rank, world, local_rank, dist):
 
     if rank != 0:
         return None
-    cpu_jobs = []
-    for i in range(60):
-        uv, vals = slice_of(pools, specs, i)
-        cpu_jobs.append((uv, vals, gcfs[int(specs["S"][i])], int(specs["side"][i]),
-                         int(specs["S"][i])))
-    cv, cn, cs, ct = cpu_rate(cpu_jobs, args.cpu_budget)
     best_plain = max(plain.values())
     res = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mvis/s", "n_gpus": world,
@@ -601,9 +689,7 @@ def run_served(args, rank, world, local_rank, dist):
         "latency_sweep": sweep,
         "accuracy": acc,
         "roofline": roof,
-        "cpu_baseline": {"value": round(cv, 4), "unit": "Mvis/s", "cores": ct, "kind": "port",
-                         "sample": f"first requests of the stream, {cn} visibilities "
-                                   f"({cs:.1f} s), gridCPU_pz restatement over {ct} row bands"},
+        "cpu_baseline": cpu_baseline(w, rank),
         "e2e": e2e,
         "gpu_launches": int(launches),
     }
@@ -627,7 +713,8 @@ def run_batch(args, rank, world, local_rank, dist):
         # a small case of the same kernel for detailed profiler captures:
         # 64 jobs from 2 observations per grid side (about 1.5 GB on the device)
         n = 64
-    pools, specs, gcfs = stream_inputs(n, seed=17 + rank, nsets=2 if args.profile_small else 8)
+    pools, specs, gcfs = stream_inputs(n, seed=stream_seed("batch", rank),
+                                       nsets=2 if args.profile_small else 8)
     total_vis = int(specs["nvis"].sum())
     dp = DevicePools(pools, dev)
     dg = {S: torch.from_numpy(gcfs[S].reshape(-1)).to(dev) for S in (8, 16)}
@@ -755,12 +842,6 @@ def run_batch(args, rank, world, local_rank, dist):
                       "slots, batches of up to 64 jobs)"}
     if rank != 0:
         return None
-    cpu_jobs = []
-    for i in range(40):
-        uv, vals = slice_of(pools, specs, i)
-        cpu_jobs.append((uv, vals, gcfs[int(specs["S"][i])], int(specs["side"][i]),
-                         int(specs["S"][i])))
-    cv, cn, cs_, ct = cpu_rate(cpu_jobs, args.cpu_budget)
     res = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mvis/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
@@ -776,9 +857,7 @@ def run_batch(args, rank, world, local_rank, dist):
         "plain_per_job_Mvis_per_s": plain,
         "speedup_vs_best_plain": round(value / world / max(plain.values()), 2),
         "flags": flags, "accuracy": acc, "roofline": roof,
-        "cpu_baseline": {"value": round(cv, 4), "unit": "Mvis/s", "cores": ct, "kind": "port",
-                         "sample": f"first jobs, {cn} visibilities ({cs_:.1f} s), gridCPU_pz "
-                                   f"restatement over {ct} row bands"},
+        "cpu_baseline": cpu_baseline(w, rank),
         "e2e": e2e, "gpu_launches": int(launches),
     }
     clocks = clk.summary()
@@ -845,21 +924,31 @@ def run_single(args, rank, world, local_rank, dist):
     flags = ctx.read_flags()
     err = None
     if rank == 0 and not args.no_check:
-        nchk = n if (N <= 4096 or w.get("precision_study")) else n // 16
-        ref = O.grid_pz(uv[:nchk], pairs(vals[:nchk]), pairs(gcf), N, S, nthreads=os.cpu_count())
-        den = max(np.abs(ref).max(), 1e-300)
-        rden = np.sqrt((ref ** 2).sum())
+        B = w.get("check_window")
+        if B:
+            # the oracle of a central B x B window: every visibility that can
+            # reach it, on a shifted (B + 2S)^2 grid
+            x0 = y0 = N // 2 - B // 2
+            ref, mag, nsub = window_reference(uv, vals, gcf, N, S, x0, y0, B)
+            checked = (f"central {B}x{B} window of the grid (cells [{x0}, {x0 + B})^2), "
+                       f"against the oracle of the {nsub} visibilities that reach it")
+        else:
+            x0 = y0 = 0
+            B = N
+            ref, mag = oracle_pair(uv, vals, gcf, N, S)
+            checked = f"whole grid, all {n} visibilities"
 
         def error_of(opts, grid=out):
-            ctx.grid(opts, grid, d_uv[:nchk], d_vals[:nchk], d_gcf, N, S)
-            got = torch.view_as_real(grid).reshape(N, N, 2).cpu().numpy().astype(np.float64)
-            d = max(np.abs(got[..., 0] - ref[0, 0]).max(), np.abs(got[..., 1] - ref[1, 0]).max())
-            rms = np.sqrt(((got[..., 0] - ref[0, 0]) ** 2 + (got[..., 1] - ref[1, 0]) ** 2).sum())
-            return {"max_rel": float(d / den), "rms_rel": float(rms / rden)}
+            ctx.grid(opts, grid, d_uv, d_vals, d_gcf, N, S)
+            got = torch.view_as_real(grid).reshape(N, N, 2)[y0:y0 + B, x0:x0 + B]
+            got = got.cpu().numpy().astype(np.float64)
+            a = ErrAcc()
+            a.add(np.moveaxis(got, -1, 0).reshape(2, 1, B, B), ref, mag)
+            return a.result()
 
         err = error_of(o)
-        err["visibilities_checked"] = int(nchk)
-        err["reference"] = "FP64 oracle (gridCPU_pz restatement)"
+        err["checked"] = checked
+        err["metrics"] = ACC_NOTE
         if w.get("precision_study") and w["vals"] == "c64":
             # the precision form: the same visibilities with plain FP32 sums,
             # into the workload's complex128 grid and into a complex64 grid
@@ -871,7 +960,7 @@ def run_single(args, rank, world, local_rank, dist):
                 "complex64_grid": {"fp32_compensated": error_of(o, out64),
                                    "fp32_plain": error_of(plain, out64)}}
             del out64
-        del ref
+        del ref, mag
     start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     kern_ms, bin_ms = [], []
@@ -928,7 +1017,6 @@ def run_single(args, rank, world, local_rank, dist):
     else:
         alg = n * (8 + vb) + 2 * N * N * ob
     mean_kern = statistics.mean(kern_ms)
-    cv, cn, cs, ct = cpu_rate([(uv[:1 << 20], vals[:1 << 20], gcf, N, S)], args.cpu_budget)
     res = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mvis/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -947,9 +1035,7 @@ def run_single(args, rank, world, local_rank, dist):
         "accuracy": err, "flags": flags,
         "roofline": roofline(f"{mode_name}_kernel", alg, mean_kern,
                              f"{mode_name}_{args.workload}", n * S * S, local_rank),
-        "cpu_baseline": {"value": round(cv, 4), "unit": "Mvis/s", "cores": ct, "kind": "port",
-                         "sample": f"first {cn} visibilities of the workload ({cs:.1f} s), "
-                                   f"gridCPU_pz restatement over {ct} row bands"},
+        "cpu_baseline": cpu_baseline(w, rank),
         "e2e": e2e, "gpu_launches": int(launches),
     }
     clocks = clk.summary()
@@ -1096,40 +1182,15 @@ def run_reference(args, rank, world):
         return {"impl": "reference",
                 "unavailable": "the reference has no degridder (it grids only)"}
     threads = os.cpu_count() or 1
-    if w["kind"] == "single":
-        uv, vals, gcf = make_single(w, seed=1000)
-        jobs = [(uv, vals, gcf, w["N"], w["S"])]
-        desc_n = w["npts"]
-    else:
-        pools, specs, gcfs = stream_inputs(w["n"], seed=7)
-        jobs = []
-        for i in range(w["n"]):
-            uv, vals = slice_of(pools, specs, i)
-            jobs.append((uv, vals, gcfs[int(specs["S"][i])], int(specs["side"][i]),
-                         int(specs["S"][i])))
-        desc_n = int(specs["nvis"].sum())
-    # a step grids whole jobs (or a prefix of a single job) for about
-    # cpu_budget / steps seconds
-    per_step = max(0.5, args.cpu_budget / max(1, args.steps))
+    # every step grids the workload's CPU sample -- the same sample as the
+    # cpu_baseline of the GPU arm's line
+    jobs, desc = cpu_sample(w)
+    desc_n = (w["npts"] if w["kind"] == "single"
+              else int(stream_inputs(w["n"], seed=stream_seed(w["kind"]))[1]["nvis"].sum()))
 
     def step():
-        vis, t0 = 0, time.perf_counter()
-        for uv, vals, gcf, N, S in jobs:
-            if w["kind"] == "single":
-                # prefix sized to the budget (measured on the first step)
-                m = min(len(uv), step.prefix)
-                O.grid_pz(uv[:m], pairs(vals[:m]), pairs(gcf), N, S, nthreads=threads)
-                vis += m
-            else:
-                O.grid_pz(uv, pairs(vals), pairs(gcf), N, S, nthreads=threads)
-                vis += len(uv)
-            if time.perf_counter() - t0 >= per_step:
-                break
-        return vis, time.perf_counter() - t0
-    step.prefix = 1 << 16
-    if w["kind"] == "single":
-        v, dt = step()
-        step.prefix = int(min(len(jobs[0][0]), max(1 << 12, v * per_step / max(dt, 1e-6))))
+        _, vis, t, _ = cpu_rate(jobs, threads)
+        return vis, t
     for _ in range(args.warmup):
         step()
     tot_v, tot_t = 0, 0.0
@@ -1147,13 +1208,64 @@ def run_reference(args, rank, world):
         "config": {"workload": f"{args.workload}: {w['desc']}", "visibilities_per_pass": desc_n},
         "cpu_baseline": {"value": round(val, 4), "unit": "Mvis/s", "cores": threads,
                          "kind": "port",
-                         "sample": f"{tot_v // max(1, args.steps)} visibilities per step (a bounded "
-                                   f"prefix of the workload); gridCPU_pz restatement "
+                         "sample": f"every step: {desc}; gridCPU_pz restatement "
                                    f"(oracle/grid_oracle.c) over {threads} row bands, "
                                    f"bit-identical to the single-threaded reference"},
         "e2e": {"value": round(val, 4), "unit": "Mvis/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+
+
+# ---------------------------------------------------------------------------
+# the other configurations, compact, in the default line
+# ---------------------------------------------------------------------------
+SUB_CONFIGS = (("uniform1024", None), ("tracks4096", None), ("tracks4096", "scatter"),
+               ("tracks4096", "gather"), ("disk8192", None), ("batch256", None))
+
+
+def compact(res):
+    """the figures of a full result line that the default line carries for
+    the other configurations"""
+    keep = ("value", "unit", "ms_per_step", "steps", "dtype", "speedup_vs_best_plain",
+            "plain_per_job_Mvis_per_s", "tap_updates_per_s", "phase_ms", "flags",
+            "gpu_launches")
+    out = {k: res[k] for k in keep if k in res}
+    out["workload"] = res["config"]["workload"]
+    if "method" in res["config"]:
+        out["method"] = res["config"]["method"]
+    acc = res.get("accuracy")
+    if acc:
+        out["accuracy"] = {k: v for k, v in acc.items() if k not in ("metrics", "reference")}
+    if res.get("e2e"):
+        out["e2e"] = {k: res["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step",
+                                                 "d2h_bytes_per_step", "ms_per_step")}
+    r = res.get("roofline") or {}
+    out["roofline"] = {k: r.get(k) for k in ("kernel", "achieved", "peak", "frac", "traffic")}
+    cb = res.get("cpu_baseline") or {}
+    out["cpu_baseline"] = {k: cb.get(k) for k in ("value", "cores", "sample")}
+    if res.get("clocks"):
+        out["clocks"] = {k: res["clocks"][k] for k in ("sm_mhz", "sm_max_mhz", "reasons")}
+    return out
+
+
+def run_configs(args, rank, world, local_rank, dist):
+    """BASELINE configurations 1-4 at a few steps each (the default line's
+    headline is configuration 5, the served stream)"""
+    import copy
+    out = {}
+    for name, method in SUB_CONFIGS:
+        a = copy.copy(args)
+        a.workload, a.method = name, method
+        a.steps, a.warmup = min(args.steps, 5), 3
+        kind = WORKLOADS[name]["kind"]
+        fn = {"batch": run_batch, "single": run_single}[kind]
+        t0 = time.perf_counter()
+        res = fn(a, rank, world, local_rank, dist)
+        if res is not None:
+            key = name + (f"_{method}" if method else "")
+            out[key] = compact(res)
+            out[key]["bench_wall_s"] = round(time.perf_counter() - t0, 1)
+    return out
 
 
 def main():
@@ -1164,7 +1276,7 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=8.0,
-                    help="seconds of CPU gridding for the CPU baseline")
+                    help="degrid4096: seconds of CPU degridding for its CPU baseline")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--profile-small", action="store_true",
@@ -1173,6 +1285,9 @@ def main():
     ap.add_argument("--method", choices=["scatter", "gather", "window"], default=None,
                     help="single-job workloads: grid with this method instead of the "
                          "workload's own")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="default workload: leave out the compact results of the other "
+                         "configurations")
     args = ap.parse_args()
     if args.warmup < 3:
         log("bench: warm-up below 3 steps; using 3")
@@ -1194,6 +1309,15 @@ def main():
         fn = {"served": run_served, "batch": run_batch, "single": run_single,
               "degrid": run_degrid}[kind]
         res = fn(args, rank, world, local_rank, dist)
+        if (args.workload == DEFAULT_WORKLOAD and world == 1 and not args.no_configs
+                and args.method is None):
+            sub = run_configs(args, rank, world, local_rank, dist)
+            if res is not None:
+                res["configs"] = sub
+                res["configs_note"] = (
+                    "BASELINE configurations 1-4 measured in the same run, min(steps, 5) "
+                    "timed steps each after 3 warm-up steps; every entry keeps the fields "
+                    "of its own full line (python bench.py --workload NAME)")
         if dist:
             dist.destroy_process_group()
     if res is not None and rank == 0:
