@@ -646,7 +646,7 @@ def run_served(args, rank, world, local_rank, dist):
         import torch as _t
         hp = {N: (_t.from_numpy(uv).pin_memory().numpy(), _t.from_numpy(v).pin_memory().numpy())
               for N, (uv, v) in pools.items()}
-        RING = 64
+        RING = args.e2e_ring
         hout = {N: [_t.empty(N * N, dtype=_t.complex64).pin_memory() for _ in range(RING)]
                 for N in hp}
         hreqs, hbuf = [], []
@@ -1333,6 +1333,9 @@ def main():
     ap.add_argument("--method", choices=["scatter", "gather", "window"], default=None,
                     help="single-job workloads: grid with this method instead of the "
                          "workload's own")
+    ap.add_argument("--e2e-ring", type=int, default=64,
+                    help="served10k e2e: pinned host output buffers per grid side that the "
+                         "client cycles through (requests in flight <= 4 x this)")
     ap.add_argument("--profile-batch", action="store_true",
                     help="served10k: only its roofline batch (the first 256 requests in one "
                          "batched call), for profiler captures")

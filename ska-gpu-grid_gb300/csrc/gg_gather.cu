@@ -2,18 +2,29 @@
 // grid_gpu.cu:391-503), rebuilt for sm_103a.
 //
 // One CTA per 32x32-cell output tile; every thread owns 4 cells (one column,
-// rows 8 apart) and sums, in registers, every tap that lands on them.  The
-// visibilities come from the tile's own uv bin and its 8 neighbours (a
-// footprint reaches at most S/2 <= 32 cells past its bin): each bin is
-// streamed through shared memory by 1-D TMA bulk copies, and a ballot
-// compaction keeps only the visibilities whose footprint overlaps the tile.
+// 4 consecutive rows: warp w owns the row band 4w..4w+3 of the tile) and
+// sums, in registers, every tap that lands on them.  The visibilities come
+// from the tile's own uv bin and its 8 neighbours (a footprint reaches at
+// most S/2 <= 32 cells past its bin): each bin is streamed through shared
+// memory by 1-D TMA bulk copies, and every warp compacts, with ballots, the
+// records of a chunk whose footprint overlaps its own band into a list of its
+// own -- a footprint of S rows reaches about S/4 + 1 of the 8 bands, and a
+// warp never visits the records that miss it.  Warps synchronise only once
+// per chunk (before its buffer is refilled).
 // Each output cell is then written exactly once with a plain store: no
 // atomics, no pre-zeroed grid, and a fixed summation order per cell.
+#include <type_traits>
+
 #include "gg_kernels.cuh"
 
 namespace gg {
 
 constexpr int kGatherChunk = 512;
+// FP32 values: every cell keeps a packed (re, im) register run, added into a
+// compensated (hi, lo) pair by TwoSum after at most this many records (a cell
+// receives at most one tap per record), so a tap costs one or two packed
+// fused multiply-adds instead of a two-sum per component
+constexpr int kGatherRun = 32;
 constexpr int kGatherTile = 32;
 constexpr int kGatherThreads = 256;
 
@@ -21,8 +32,10 @@ template <typename VT2>
 struct GatherShape {
   static constexpr int IDX_BUF = kGatherChunk * 8 + 16;
   static constexpr int VAL_BUF = kGatherChunk * (int)sizeof(VT2) + 16;
+  // per-warp lists of record indices (16 bits: a chunk has at most 512)
+  static constexpr int LIST_BYTES = (kGatherThreads / 32) * kGatherChunk * 2;
   static constexpr size_t smem(int S) {
-    return 16 + 2 * IDX_BUF + 2 * VAL_BUF + kGatherChunk * 4 + 64 * S * 4;
+    return 16 + 2 * IDX_BUF + 2 * VAL_BUF + LIST_BYTES + 64 * S * 4;
   }
 };
 
@@ -41,6 +54,8 @@ __global__ void __launch_bounds__(kGatherThreads)
   using VT = typename ACC::VT;
   using VT2 = typename vec2_of<VT>::type;
   using Sh = GatherShape<VT2>;
+  constexpr bool F32 = std::is_same<VT, float>::value;
+  constexpr bool COMP = std::is_same<ACC, AccComp>::value;
   constexpr int K = kGatherChunk, H = S / 2, TT = kGatherTile;
   // unsorted input declared sorted: holes in this call's sorted records, the
   // call fails with GG_ERR_UNSORTED -- grid nothing
@@ -50,9 +65,10 @@ __global__ void __launch_bounds__(kGatherThreads)
   // double buffers, addressed arithmetically (buffer b at +b*size)
   unsigned char *const idx0 = smem + 16;
   unsigned char *const val0 = smem + 16 + 2 * Sh::IDX_BUF;
-  int *list = reinterpret_cast<int *>(smem + 16 + 2 * Sh::IDX_BUF + 2 * Sh::VAL_BUF);
-  float *g1 = reinterpret_cast<float *>(list + K);
-  __shared__ int wcount[kGatherThreads / 32 + 1];
+  unsigned short *wlist = reinterpret_cast<unsigned short *>(
+      smem + 16 + 2 * Sh::IDX_BUF + 2 * Sh::VAL_BUF) + (threadIdx.x >> 5) * K;
+  float *g1 = reinterpret_cast<float *>(smem + 16 + 2 * Sh::IDX_BUF + 2 * Sh::VAL_BUF +
+                                        Sh::LIST_BYTES);
   __shared__ int s_abort;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -79,7 +95,7 @@ __global__ void __launch_bounds__(kGatherThreads)
     const int N = J.N, log2G = J.log2G, ntx = J.ntx;
     const int tx = lt % ntx, ty = lt / ntx;
     const int x0 = tx * TT, y0 = ty * TT;
-    const int cx = x0 + lane, cy0 = y0 + warp;
+    const int cx = x0 + lane, cy0 = y0 + 4 * warp;
     GcfSrc<S, GAUSS, VT> gsrc;
     if constexpr (GAUSS) {
       gsrc.g1 = g1;
@@ -89,9 +105,28 @@ __global__ void __launch_bounds__(kGatherThreads)
     }
     for (int p = 0; p < P; ++p) {
       const VT2 *vplane = reinterpret_cast<const VT2 *>(J.vals) + (size_t)p * J.vstride;
-      ACC acc[4];
+      ACC acc[4];                          // FP64 values
+      u64 run2[4], hi2[4], lo2[4];         // FP32 values: run, compensated pair
+      int since = 0;                       // records visited since the last merge
 #pragma unroll
-      for (int k = 0; k < 4; ++k) acc[k].zero();
+      for (int k = 0; k < 4; ++k) {
+        acc[k].zero();
+        run2[k] = hi2[k] = lo2[k] = 0ull;
+      }
+      // add the register runs into the (hi, lo) pairs (compensated), or keep
+      // them as the sums (plain FP32)
+      auto merge_runs = [&]() {
+        if constexpr (COMP) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            u64 e;
+            hi2[k] = two_sum2(hi2[k], run2[k], e);
+            lo2[k] = add2(lo2[k], e);
+            run2[k] = 0ull;
+          }
+        }
+        since = 0;
+      };
       for (int by = max(ty - 1, 0); by <= min(ty + 1, ntx - 1); ++by)
         for (int bx = max(tx - 1, 0); bx <= min(tx + 1, ntx - 1); ++bx) {
           const int bin = by * ntx + bx;
@@ -123,79 +158,105 @@ __global__ void __launch_bounds__(kGatherThreads)
             const int m = min(K, s_end - s0);
             const int2 *ib = reinterpret_cast<const int2 *>((idx0 + b * Sh::IDX_BUF) + (((size_t)s0 * 8) & 15));
             const VT2 *vb = reinterpret_cast<const VT2 *>((val0 + b * Sh::VAL_BUF) + (((size_t)s0 * sizeof(VT2)) & 15));
-            // compaction: records whose footprint overlaps this tile, in order
+            // this warp's records: footprint (columns mx-H+1 .. mx+H, rows
+            // my-H+1 .. my+H) overlapping the tile's columns and the warp's
+            // rows cy0 .. cy0+3, in chunk order
             int base = 0;
-            for (int r0 = 0; r0 < m; r0 += kGatherThreads) {
-              const int r = r0 + tid;
+            for (int r0 = 0; r0 < m; r0 += 32) {
+              const int r = r0 + lane;
               bool keep = false;
               if (r < m) {
-                int2 pk = ib[r];
-                int mx = unpack_main(pk.x, log2G), my = unpack_main(pk.y, log2G);
+                const int2 pk = ib[r];
+                const int mx = unpack_main(pk.x, log2G), my = unpack_main(pk.y, log2G);
                 keep = (mx + H >= x0) && (mx - H + 1 < x0 + TT) &&
-                       (my + H >= y0) && (my - H + 1 < y0 + TT);
+                       (my + H >= cy0) && (my - H + 1 <= cy0 + 3);
               }
-              unsigned bal = __ballot_sync(0xffffffffu, keep);
-              if (lane == 0) wcount[warp] = __popc(bal);
-              __syncthreads();
-              if (tid == 0) {
-                int acc_c = 0;
-                for (int w2 = 0; w2 < kGatherThreads / 32; ++w2) {
-                  int c2 = wcount[w2];
-                  wcount[w2] = acc_c;
-                  acc_c += c2;
-                }
-                wcount[kGatherThreads / 32] = acc_c;
-              }
-              __syncthreads();
-              if (keep)
-                list[base + wcount[warp] + __popc(bal & ((1u << lane) - 1))] = r;
-              base += wcount[kGatherThreads / 32];
-              __syncthreads();
+              const unsigned bal = __ballot_sync(0xffffffffu, keep);
+              if (keep) wlist[base + __popc(bal & ((1u << lane) - 1))] = (unsigned short)r;
+              base += __popc(bal);
             }
+            __syncwarp();
             for (int q = 0; q < base; ++q) {
-              const int r = list[q];
+              if constexpr (F32) {  // uniform over the warp
+                if (++since > kGatherRun) merge_runs();
+              }
+              const int r = wlist[q];
               const int2 pk = ib[r];
+              const int my = unpack_main(pk.y, log2G);
               const int mx = unpack_main(pk.x, log2G), sx = unpack_sub(pk.x, log2G);
-              const int my = unpack_main(pk.y, log2G), sy = unpack_sub(pk.y, log2G);
+              const int sy = unpack_sub(pk.y, log2G);
               const int ap = cx - (mx - H + 1);
               if ((unsigned)ap >= (unsigned)S) continue;
               const VT2 v = vb[r];
+              if constexpr (F32) {
+                const u64 vv = pk2(v.x, v.y), vrr = pk2(v.x, v.x), vsn = pk2(-v.y, v.y);
 #pragma unroll
-              for (int k = 0; k < 4; ++k) {
-                const int bp = cy0 + 8 * k - (my - H + 1);
-                if ((unsigned)bp < (unsigned)S) {
-                  VT gr, gi, tr, ti;
-                  gsrc.value(sx, sy, ap, bp, gr, gi);
-                  if constexpr (GAUSS) {
-                    tr = v.x * gr;
-                    ti = v.y * gr;
-                  } else {
-                    cmul<VT>(v.x, v.y, gr, gi, tr, ti);
+                for (int k = 0; k < 4; ++k) {
+                  const int bp = cy0 + k - (my - H + 1);
+                  if ((unsigned)bp < (unsigned)S) {
+                    VT gr, gi;
+                    gsrc.value(sx, sy, ap, bp, gr, gi);
+                    if constexpr (GAUSS) {
+                      run2[k] = fma2(vv, pk2(gr, gr), run2[k]);
+                    } else {
+                      // (vr gr - vi gi, vr gi + vi gr), two packed roundings
+                      run2[k] = fma2(vrr, pk2(gr, gi), fma2(vsn, pk2(gi, gr), run2[k]));
+                    }
                   }
-                  acc[k].add(tr, ti);
+                }
+              } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                  const int bp = cy0 + k - (my - H + 1);
+                  if ((unsigned)bp < (unsigned)S) {
+                    VT gr, gi, tr, ti;
+                    gsrc.value(sx, sy, ap, bp, gr, gi);
+                    if constexpr (GAUSS) {
+                      tr = v.x * gr;
+                      ti = v.y * gr;
+                    } else {
+                      cmul<VT>(v.x, v.y, gr, gi, tr, ti);
+                    }
+                    acc[k].add(tr, ti);
+                  }
                 }
               }
             }
-            __syncthreads();  // buffer b and the list fully consumed
+            __syncthreads();  // buffer b consumed by every warp
             if (tid == 0 && c + 2 < nchunks) issue(c + 2, b);
           }
           if (s_abort) by = ntx;  // leave both bin loops
           if (s_abort) break;
         }
       if (s_abort) break;
+      if constexpr (F32) merge_runs();
       // each cell written once: plain stores, coalesced along x
       const size_t NN = (size_t)N * N;
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const int cy = cy0 + 8 * k;
+        const int cy = cy0 + k;
         if (cx < N && cy < N) {
           size_t cell = (size_t)cy * N + cx;
+          double dre, dim;
+          float fre, fim;
+          if constexpr (F32) {
+            // compensated: hi + lo (exact in FP64, rounded once in FP32);
+            // plain: the register run holds the sum
+            const float2 h = upk2(COMP ? hi2[k] : run2[k]), l = upk2(lo2[k]);
+            dre = (double)h.x + (double)l.x;
+            dim = (double)h.y + (double)l.y;
+            fre = __fadd_rn(h.x, l.x);
+            fim = __fadd_rn(h.y, l.y);
+          } else {
+            dre = acc[k].dre();
+            dim = acc[k].dim();
+            fre = acc[k].fre();
+            fim = acc[k].fim();
+          }
           if (J.out_f64)
-            grid_store<double>((double *)J.out, cell, p, P, NN, J.planar,
-                               acc[k].dre(), acc[k].dim());
+            grid_store<double>((double *)J.out, cell, p, P, NN, J.planar, dre, dim);
           else
-            grid_store<float>((float *)J.out, cell, p, P, NN, J.planar,
-                              acc[k].fre(), acc[k].fim());
+            grid_store<float>((float *)J.out, cell, p, P, NN, J.planar, fre, fim);
         }
       }
     }

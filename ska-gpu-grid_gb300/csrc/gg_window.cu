@@ -48,46 +48,6 @@
 
 namespace gg {
 
-// ---- packed FP32x2 helpers (PTX f32x2, sm_100+) ------------------------------
-typedef unsigned long long u64;
-__device__ __forceinline__ u64 pk2(float a, float b) {
-  u64 r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-  return r;
-}
-__device__ __forceinline__ float2 upk2(u64 r) {
-  float2 f;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(f.x), "=f"(f.y) : "l"(r));
-  return f;
-}
-__device__ __forceinline__ u64 add2(u64 a, u64 b) {
-  u64 d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ u64 sub2(u64 a, u64 b) {
-  u64 d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ u64 mul2(u64 a, u64 b) {
-  u64 d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ u64 fma2(u64 a, u64 b, u64 c) {
-  u64 d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
-// (s, e) = TwoSum(a, b) on both lanes: s = fl(a+b), a + b = s + e exactly
-__device__ __forceinline__ u64 two_sum2(u64 a, u64 b, u64 &e) {
-  const u64 s = add2(a, b);
-  const u64 bb = sub2(s, a);
-  e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
-  return s;
-}
-
 // ---- per-thread running sums and sub-grid cells -------------------------------
 // MODE 0: plain FP32      sum u64 (re, im)          cell float2
 // MODE 1: compensated     sums u64 hi, lo           cell float4 {hi, lo}
