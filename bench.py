@@ -632,7 +632,7 @@ def run_served(args, rank, world, local_rank, dist):
     nv = sum(j.npts for j in jobs)
     alg = nv * 16 + sum(2 * 8 * j.img_dim * j.img_dim for j in jobs)
     taps = sum(j.npts * j.gcf_dim * j.gcf_dim for j in jobs)
-    roof = roofline("window_kernel", alg, kern_ms, "window_batch256", taps, local_rank)
+    roof = roofline("window_kernel", alg, kern_ms, "window_served256", taps, local_rank)
 
     # e2e: host requests through the server's host path -- inputs copied in
     # from pinned host memory and every grid copied back to pinned host

@@ -597,7 +597,10 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
   pl.gcf_copies.clear();
   pl.hgcf_off.assign(njobs, SIZE_MAX);
   pl.hgcf_copy.assign(njobs, SIZE_MAX);
-  if (mode == GG_MODE_WINDOW && !pl.gauss) {
+  // row-doubled copies of the tables (moving window), and for complex64
+  // tables their real parts with a "has an imaginary part" flag (moving
+  // window and gather take a real-factor path when it is clear)
+  if ((mode == GG_MODE_WINDOW || (mode == GG_MODE_GATHER && !pl.vals_f64)) && !pl.gauss) {
     std::map<std::tuple<const void *, int, int>, size_t> seen;  // -> copy index
     for (int k = 0; k < njobs; ++k) {
       const gg_job &J = jobs[order[k]];
@@ -754,7 +757,9 @@ static void plan_bind(const gg_options *opt, Plan &pl, char *ws, char *host) {
     }
     if (pl.hgcf_off[k] != SIZE_MAX) {
       const auto &c = pl.gcf_copies[pl.hgcf_copy[k]];
-      D.gcf = ws + c.off;
+      // the gather kernel reads the caller's [G*G][S][S] table (and the real
+      // parts of the copy); the moving window reads the row-doubled copy
+      if (pl.mode == GG_MODE_WINDOW) D.gcf = ws + c.off;
       D.gcf_real = c.off_real ? (const float *)(ws + c.off_real) : nullptr;
       D.gcf_imag = c.off_real ? (const int *)(ws + pl.o_gcf_flags) + pl.hgcf_copy[k] : nullptr;
     }

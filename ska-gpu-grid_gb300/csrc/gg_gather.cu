@@ -103,6 +103,11 @@ __global__ void __launch_bounds__(kGatherThreads)
       gsrc.tab = reinterpret_cast<const VT2 *>(J.gcf);
       gsrc.G = J.G;
     }
+    // complex64 table without imaginary parts (flagged on the device when
+    // the real parts were copied, rows doubled: [G*G][2S][S]): a tap is one
+    // float load and one packed fused multiply-add
+    const float *const greal =
+        F32 && !GAUSS && J.gcf_real && J.gcf_imag && *J.gcf_imag == 0 ? J.gcf_real : nullptr;
     for (int p = 0; p < P; ++p) {
       const VT2 *vplane = reinterpret_cast<const VT2 *>(J.vals) + (size_t)p * J.vstride;
       ACC acc[4];                          // FP64 values
@@ -188,6 +193,22 @@ __global__ void __launch_bounds__(kGatherThreads)
               const int ap = cx - (mx - H + 1);
               if ((unsigned)ap >= (unsigned)S) continue;
               const VT2 v = vb[r];
+              if constexpr (F32 && !GAUSS) {
+                if (greal) {  // uniform over the tile
+                  const u64 vv = pk2(v.x, v.y);
+                  const float *gp = greal + (size_t)(sy * J.G + sx) * (2 * S * S) + ap +
+                                    (cy0 - (my - H + 1)) * S;
+#pragma unroll
+                  for (int k = 0; k < 4; ++k) {
+                    const int bp = cy0 + k - (my - H + 1);
+                    if ((unsigned)bp < (unsigned)S) {
+                      const float g = __ldg(gp + k * S);
+                      run2[k] = fma2(vv, pk2(g, g), run2[k]);
+                    }
+                  }
+                  continue;
+                }
+              }
               if constexpr (F32) {
                 const u64 vv = pk2(v.x, v.y), vrr = pk2(v.x, v.x), vsn = pk2(-v.y, v.y);
 #pragma unroll
