@@ -55,11 +55,11 @@ FALLBACK_HBM_GBS = 6800.0
 
 STREAM_DESC = ("grid side uniform in {256,512,1024,2048}; support 8 or 16, "
                "oversample 8; visibility count lognormal (log10 ~ N(5, 0.5)) "
-               "clipped to [1e4, 1e6]; each a contiguous slice (whole baseline "
-               "tracks) of one of 8 synthetic observations per grid side with "
-               "the tracks4096 geometry (64 antennas at random positions in a "
-               "2 km disk, 2016 baselines x 2080 samples over +-4 h, dec -30 "
-               "deg, 90% fill); complex64 N(0,1) values; FP64 "
+               "clipped to [1e4, 1e6]; every job its own observation with the "
+               "tracks4096 geometry: its own 64 antennas at random positions in "
+               "a 2 km disk, whole tracks of a random choice of its 2016 "
+               "baselines, 2080 samples over +-4 h, dec -30 deg, the longest "
+               "baseline at 90% fill; complex64 N(0,1) values; FP64 "
                "u,v; complex64 grids; FP32 compensated accumulation; "
                "tabulated separable Gaussian GCFs resident on the device")
 
@@ -296,15 +296,15 @@ def cpu_sample(w, rank=0):
         m = min(len(uv), (1 << 18) if w["S"] >= 32 else (1 << 20))
         return ([(uv[:m], vals[:m], gcf, w["N"], w["S"])],
                 f"the first {m} visibilities of the workload")
-    pools, specs, gcfs = stream_inputs(w["n"], seed=stream_seed(w["kind"], rank))
+    st = JobStream(w["n"], stream_seed(w["kind"], rank))
     jobs, vis = [], 0
     for i in range(w["n"]):
-        uv, vals = slice_of(pools, specs, i)
-        if jobs and vis + len(uv) > CPU_SAMPLE_VIS:
+        N, S, n = st.shape(i)
+        if jobs and vis + n > CPU_SAMPLE_VIS:
             break
-        jobs.append((uv, vals, gcfs[int(specs["S"][i])], int(specs["side"][i]),
-                     int(specs["S"][i])))
-        vis += len(uv)
+        uv, vals = st.host_job(i)
+        jobs.append((uv, vals, st.gcfs[S], N, S))
+        vis += n
     return jobs, f"the first {len(jobs)} jobs of the stream ({vis} visibilities)"
 
 
@@ -334,147 +334,97 @@ def cpu_baseline(w, rank=0):
 # ---------------------------------------------------------------------------
 # shared pieces of the batched and served workloads
 # ---------------------------------------------------------------------------
-def stream_inputs(n, seed, nsets=8):
-    import synth
-    pools = synth.track_pool(seed=seed, nsets=nsets)
-    specs = synth.request_specs(n, seed=seed + 1, nsets=nsets)
-    gcfs = {S: synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64) for S in (8, 16)}
-    return pools, specs, gcfs
+class JobStream:
+    """The jobs of the batched and served workloads: shapes from
+    synth.request_specs (grid side, support, visibility count), and for every
+    job its own observation -- its own random 64-antenna array, tracks of a
+    random choice of its baselines (synth.job_tracks, seeded with the job's
+    index) -- generated with torch on the GPU when there is one, else on the
+    host, once per job and kept."""
 
-
-def slice_of(pools, specs, i):
-    N, s, off, n = (int(specs[k][i]) for k in ("side", "set", "offset", "nvis"))
-    uv, vals = pools[N]
-    return uv[s, off:off + n], vals[s, off:off + n]
-
-
-class DevicePools:
-    """track pools on the device; pointers into them for each request"""
-
-    def __init__(self, pools, dev):
+    def __init__(self, n, seed, device=None):
+        import synth
         import torch
-        self.t = {N: (torch.from_numpy(uv).to(dev), torch.from_numpy(v).to(dev))
-                  for N, (uv, v) in pools.items()}
-        self.len = {N: uv.shape[1] for N, (uv, _) in pools.items()}
+        self.specs = synth.request_specs(n, seed=seed + 1)
+        self.seed = seed
+        self.n = n
+        self.device = device or ("cuda" if torch.cuda.is_available() else "cpu")
+        self.gcfs = {S: synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+                     for S in (8, 16)}
+        self.dev = {}
 
-    def ptrs(self, N, s, off):
-        uv, v = self.t[N]
-        L = self.len[N]
-        return (uv.data_ptr() + (s * L + off) * 16, v.data_ptr() + (s * L + off) * 8)
+    def shape(self, i):
+        return (int(self.specs["side"][i]), int(self.specs["S"][i]),
+                int(self.specs["nvis"][i]))
 
+    def total_vis(self, n=None):
+        return int(self.specs["nvis"][: self.n if n is None else n].sum())
 
-ACC_NOTE = ("max_rel / rms_rel: normwise, |gpu - oracle| / max |oracle| (max) and "
-            "||gpu - oracle|| / ||oracle|| (rms) over the grid; cell_max / cell_rms: per "
-            "cell, |gpu - oracle| / sum |v||w| of the cell's additions (forward error of "
-            "each cell's sum), over the cells that receive any")
+    def device_job(self, i):
+        """(uv float64 (n, 2), vals complex64 (n,)) tensors on the device"""
+        if i not in self.dev:
+            import synth
+            N, _, n = self.shape(i)
+            self.dev[i] = synth.job_tracks(N, n, self.seed * 100003 + i, self.device)
+        return self.dev[i]
 
+    def generate(self, n=None):
+        for i in range(self.n if n is None else n):
+            self.device_job(i)
 
-class ErrAcc:
-    """normwise and per-cell error of grids against the FP64 oracle,
-    accumulated over several grids (planar (2, P, N, N) float64 each)"""
+    def ptrs(self, i):
+        uv, v = self.device_job(i)
+        return uv.data_ptr(), v.data_ptr()
 
-    def __init__(self):
-        self.worst = self.num = self.den = 0.0
-        self.cmax = self.csq = 0.0
-        self.cells = 0
+    def host_job(self, i):
+        uv, v = self.device_job(i)
+        return uv.cpu().numpy(), v.cpu().numpy()
 
-    def add(self, got, ref, mag):
-        self.worst = max(self.worst, float(np.abs(got - ref).max() /
-                                           max(np.abs(ref).max(), 1e-300)))
-        self.num += float(((got - ref) ** 2).sum())
-        self.den += float((ref ** 2).sum())
-        d = np.hypot(got[0] - ref[0], got[1] - ref[1])
-        hit = mag > 0
-        if np.any(d[~hit] != 0):
-            self.cmax = float("inf")
-        e = d[hit] / mag[hit]
-        if e.size:
-            self.cmax = max(self.cmax, float(e.max()))
-            self.csq += float((e * e).sum())
-            self.cells += int(e.size)
-
-    def result(self, **extra):
-        r = {"max_rel": self.worst, "rms_rel": (self.num / max(self.den, 1e-300)) ** 0.5,
-             "cell_max": self.cmax,
-             "cell_rms": (self.csq / max(self.cells, 1)) ** 0.5}
-        r.update(extra)
-        r["reference"] = "FP64 oracle (gridCPU_pz restatement)"
-        return r
+    def device_bytes(self):
+        return sum(uv.numel() * 8 + v.numel() * 8 for uv, v in self.dev.values())
 
 
-def oracle_pair(uv, vals, gcf, N, S):
-    """(planar FP64 grid, per-cell magnitude sums) of the oracle"""
-    import oracle as O
-    t = os.cpu_count() or 1
-    return (O.grid_pz(uv, pairs(vals), pairs(gcf), N, S, nthreads=t),
-            O.grid_mag(uv, pairs(vals), pairs(gcf), N, S, nthreads=t))
-
-
-def window_reference(uv, vals, gcf, N, S, x0, y0, B):
-    """Oracle of the B x B window [x0, x0+B) x [y0, y0+B) of an N^2 grid:
-    every visibility whose footprint can reach the window, shifted by an
-    integer offset (exact in FP64 and keeping u, v float-representable, so
-    main and oversample indices shift exactly) onto a (B + 2S)^2 grid.
-    Returns (ref, mag) of the window, planar (2, 1, B, B) and (1, B, B)."""
-    m = np.floor(uv)
-    keep = ((m[:, 0] >= x0 - S) & (m[:, 0] < x0 + B + S) &
-            (m[:, 1] >= y0 - S) & (m[:, 1] < y0 + B + S))
-    sub = uv[keep] - np.array([x0 - S, y0 - S], np.float64)
-    ref, mag = oracle_pair(sub, vals[keep], gcf, B + 2 * S, S)
-    return ref[:, :, S:S + B, S:S + B], mag[:, S:S + B, S:S + B], int(keep.sum())
-
-
-def check_sample(grids, pools, specs, gcfs, idx):
+def check_sample(grids, st, idx):
     """normwise and per-cell error of device grids vs the FP64 oracle"""
     acc = ErrAcc()
     for i, g in zip(idx, grids):
-        uv, vals = slice_of(pools, specs, i)
-        N, S = int(specs["side"][i]), int(specs["S"][i])
-        ref, mag = oracle_pair(uv, vals, gcfs[S], N, S)
+        uv, vals = st.host_job(i)
+        N, S, _ = st.shape(i)
+        ref, mag = oracle_pair(uv, vals, st.gcfs[S], N, S)
         got = np.stack([g.real, g.imag]).reshape(2, 1, N, N).astype(np.float64)
         acc.add(got, ref, mag)
     return acc.result(jobs_checked=len(idx), metrics=ACC_NOTE)
 
 
-def served_roofline_jobs(specs, n, dev, device_inputs):
-    """The first 256 requests of the stream as batch jobs (the batch the served
-    line's roofline is measured on): (jobs, grids, gcf tensors).
-    device_inputs(i) -> (uv pointer, vals pointer) of request i."""
+def stream_jobs(st, n, dev):
+    """The first n jobs of a stream as batch jobs on device inputs: (jobs,
+    grids, gcf tensors)."""
     import torch
     import gpugrid as gg
-    import synth
-    dg = {S: torch.from_numpy(synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
-                              .reshape(-1)).to(dev) for S in (8, 16)}
+    dg = {S: torch.from_numpy(st.gcfs[S].reshape(-1)).to(dev) for S in (8, 16)}
     jobs, grids = [], []
-    for i in range(min(256, n)):
-        N, S = int(specs["side"][i]), int(specs["S"][i])
-        pu, pv = device_inputs(i)
+    for i in range(n):
+        N, S, nv = st.shape(i)
+        pu, pv = st.ptrs(i)
         grids.append(torch.empty(N * N, dtype=torch.complex64, device=dev))
         j = gg.gg_job()
         j.out, j.uv, j.vals, j.gcf = grids[-1].data_ptr(), pu, pv, dg[S].data_ptr()
-        j.npts, j.img_dim, j.gcf_dim = int(specs["nvis"][i]), N, S
+        j.npts, j.img_dim, j.gcf_dim = nv, N, S
         j.uv_type, j.vals_type, j.out_type = gg.C128, gg.C64, gg.C64
         jobs.append(j)
     return jobs, grids, dg
 
 
-def profile_served_batch(args, specs, pools, opts, dev, local_rank):
+def profile_served_batch(args, st, opts, dev, local_rank):
     """--profile-batch: only the served line's roofline batch (the first 256
-    requests in one batched call), its inputs copied to the device alone
-    (about 1 GB), launched 3 times and once more inside the NVTX range
-    gg_profiled -- a case a profiler captures launch by launch.  Prints the
-    kernel time and the algorithmic bytes of that launch."""
+    requests in one batched call; only their inputs are generated, about 1
+    GB), launched 3 times and once more inside the NVTX range gg_profiled --
+    a case a profiler captures launch by launch.  Prints the kernel time and
+    the algorithmic bytes of that launch."""
     import torch
     import gpugrid as gg
-    n = min(256, len(specs["nvis"]))
-    keep = []
-
-    def device_inputs(i):
-        uv, vals = slice_of(pools, specs, i)
-        keep.append((torch.from_numpy(np.ascontiguousarray(uv)).to(dev),
-                     torch.from_numpy(np.ascontiguousarray(vals)).to(dev)))
-        return keep[-1][0].data_ptr(), keep[-1][1].data_ptr()
-    jobs, grids, _ = served_roofline_jobs(specs, n, dev, device_inputs)
+    n = min(256, st.n)
+    jobs, grids, _ = stream_jobs(st, n, dev)
     ctx = gg.Context(local_rank)
     ctx.profile(True)
     for _ in range(3):
@@ -507,23 +457,26 @@ def run_served(args, rank, world, local_rank, dist):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     n = w["n"]
-    pools, specs, gcfs = stream_inputs(n, seed=stream_seed("served", rank))
-    total_vis = int(specs["nvis"].sum())
+    js = JobStream(n, stream_seed("served", rank), dev)
+    specs, gcfs = js.specs, js.gcfs
+    total_vis = js.total_vis()
     opts = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
                       layout=gg.LAYOUT_INTERLEAVED, autotune=True)
     if args.profile_batch:
-        return profile_served_batch(args, specs, pools, opts, dev, local_rank)
-    dp = DevicePools(pools, dev)
+        return profile_served_batch(args, js, opts, dev, local_rank)
+    t_gen = time.perf_counter()
+    js.generate()
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t_gen
     srv = gg.Server(device=local_rank, streams=w["streams"], max_batch_jobs=w["max_batch_jobs"],
                     max_batch_vis=w["max_batch_vis"], hbm_budget=w["budget"], options=opts)
     gids = {S: srv.add_gcf(gcfs[S]) for S in (8, 16)}
     flags = gg.REQ_INPUTS_ON_DEVICE | gg.REQ_KEEP_RESIDENT
     reqs = []
     for i in range(n):
-        N, S = int(specs["side"][i]), int(specs["S"][i])
-        pu, pv = dp.ptrs(N, int(specs["set"][i]), int(specs["offset"][i]))
-        reqs.append(gg.Server.request(pu, pv, None, int(specs["nvis"][i]), N, S, gids[S],
-                                      flags=flags))
+        N, S, nv = js.shape(i)
+        pu, pv = js.ptrs(i)
+        reqs.append(gg.Server.request(pu, pv, None, nv, N, S, gids[S], flags=flags))
 
     def stream(offsets, keep=()):
         """submit all requests at the given arrival offsets; wait, release;
@@ -545,8 +498,8 @@ def run_served(args, rank, world, local_rank, dist):
     zeros = np.zeros(n)
     for _ in range(args.warmup):
         stream(zeros)
-    # timed saturation passes (all arrivals at t=0); L2: the 3.2 GB of input
-    # pools exceed it
+    # timed saturation passes (all arrivals at t=0); L2: the inputs (43 GB,
+    # every request its own) exceed it
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -585,7 +538,7 @@ def run_served(args, rank, world, local_rank, dist):
     # accuracy on a sample of requests, from the server's resident grids
     sample = list(range(0, n, max(1, n // 12)))[:12]
     _, _, kept = stream(zeros, keep=set(sample))
-    acc = check_sample([kept[i] for i in sample], pools, specs, gcfs, sample) \
+    acc = check_sample([kept[i] for i in sample], js, sample) \
         if rank == 0 and not args.no_check else None
 
     # plain per-request launches on one stream (no batching)
@@ -601,11 +554,11 @@ def run_served(args, rank, world, local_rank, dist):
                                  layout=gg.LAYOUT_INTERLEAVED))):
         jobs = []
         for i in range(n):
-            N, S = int(specs["side"][i]), int(specs["S"][i])
-            pu, pv = dp.ptrs(N, int(specs["set"][i]), int(specs["offset"][i]))
+            N, S, nv = js.shape(i)
+            pu, pv = js.ptrs(i)
             j = gg.gg_job()
             j.out, j.uv, j.vals, j.gcf = outs[N].data_ptr(), pu, pv, dg[S].data_ptr()
-            j.npts, j.img_dim, j.gcf_dim = int(specs["nvis"][i]), N, S
+            j.npts, j.img_dim, j.gcf_dim = nv, N, S
             j.uv_type, j.vals_type, j.out_type = gg.C128, gg.C64, gg.C64
             jobs.append(j)
         for j in jobs[:50]:
@@ -621,9 +574,7 @@ def run_served(args, rank, world, local_rank, dist):
 
     # kernel-level roofline: the first 256 requests as one profiled batch
     ctx.profile(True)
-    jobs, grid_out, _ = served_roofline_jobs(
-        specs, n, dev, lambda i: dp.ptrs(int(specs["side"][i]), int(specs["set"][i]),
-                                         int(specs["offset"][i])))
+    jobs, grid_out, _ = stream_jobs(js, min(256, n), dev)
     for _ in range(3):
         ctx.grid_batch(opts, jobs)
     with nvtx_range("gg_profiled"):
@@ -644,23 +595,31 @@ def run_served(args, rank, world, local_rank, dist):
     if not args.no_e2e:
         import collections
         import torch as _t
-        hp = {N: (_t.from_numpy(uv).pin_memory().numpy(), _t.from_numpy(v).pin_memory().numpy())
-              for N, (uv, v) in pools.items()}
+        # every request's inputs in pinned host memory (copied once from the
+        # generated device inputs, outside the timed passes)
+        h_uv = _t.empty((total_vis, 2), dtype=_t.float64).pin_memory()
+        h_v = _t.empty(total_vis, dtype=_t.complex64).pin_memory()
+        hoff, o = [], 0
+        for i in range(n):
+            uvd, vd = js.device_job(i)
+            h_uv[o:o + len(uvd)].copy_(uvd)
+            h_v[o:o + len(vd)].copy_(vd)
+            hoff.append(o)
+            o += len(uvd)
+        torch.cuda.synchronize()
+        sides = sorted({int(x) for x in specs["side"]})
         RING = args.e2e_ring
         hout = {N: [_t.empty(N * N, dtype=_t.complex64).pin_memory() for _ in range(RING)]
-                for N in hp}
+                for N in sides}
         hreqs, hbuf = [], []
-        used = {N: 0 for N in hp}
+        used = {N: 0 for N in sides}
         for i in range(n):
-            N, S = int(specs["side"][i]), int(specs["S"][i])
-            s_, off, nv_ = int(specs["set"][i]), int(specs["offset"][i]), int(specs["nvis"][i])
-            uvh, vh = hp[N]
-            L = uvh.shape[1]
+            N, S, nv_ = js.shape(i)
             b = used[N] % RING
             used[N] += 1
             hbuf.append((N, b))
-            hreqs.append(gg.Server.request(uvh.ctypes.data + (s_ * L + off) * 16,
-                                           vh.ctypes.data + (s_ * L + off) * 8,
+            hreqs.append(gg.Server.request(h_uv.data_ptr() + hoff[i] * 16,
+                                           h_v.data_ptr() + hoff[i] * 8,
                                            hout[N][b].data_ptr(), nv_, N, S, gids[S], flags=0))
 
         def host_pass():
@@ -698,7 +657,7 @@ def run_served(args, rank, world, local_rank, dist):
                 last[hbuf[k]] = k
             ks = sorted(last.values())[-4:]
             acc_h = check_sample([hout[hbuf[k][0]][hbuf[k][1]].numpy().copy() for k in ks],
-                                 pools, specs, gcfs, ks)
+                                 js, ks)
             assert acc_h["max_rel"] < 1e-6, acc_h
         t_all = max_over_ranks(t_all, dist, dev)
         e2e = {"value": round(replica_rate(total_vis * reps, world, t_all), 3), "unit": "Mvis/s",
@@ -727,7 +686,9 @@ def run_served(args, rank, world, local_rank, dist):
                    "visibilities_per_step": total_vis, "requests": n,
                    "server": {"streams": w["streams"], "max_batch_jobs": w["max_batch_jobs"],
                               "hbm_budget_bytes": int(w["budget"]), "method": "window"},
-                   "l2": "inputs (3.2 GB of track pools) exceed L2",
+                   "l2": f"inputs ({js.device_bytes() / 1e9:.1f} GB, every request its own "
+                         f"observation) exceed L2",
+                   "input_generation_s": round(t_gen, 2),
                    "timing": "server clock from first arrival to last grid ready, "
                              "per pass; device synchronised around the passes",
                    "autotune": gg.autotune_report().splitlines(),
@@ -759,26 +720,14 @@ def run_batch(args, rank, world, local_rank, dist):
     n = w["n"]
     if args.profile_small:
         # a small case of the same kernel for detailed profiler captures:
-        # 64 jobs from 2 observations per grid side (about 1.5 GB on the device)
+        # the first 64 jobs (about 1.5 GB on the device)
         n = 64
-    pools, specs, gcfs = stream_inputs(n, seed=stream_seed("batch", rank),
-                                       nsets=2 if args.profile_small else 8)
-    total_vis = int(specs["nvis"].sum())
-    dp = DevicePools(pools, dev)
-    dg = {S: torch.from_numpy(gcfs[S].reshape(-1)).to(dev) for S in (8, 16)}
+    js = JobStream(n, stream_seed("batch", rank), dev)
+    specs, gcfs = js.specs, js.gcfs
+    total_vis = js.total_vis()
     opts = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
                       layout=gg.LAYOUT_INTERLEAVED, autotune=True)
-    outs, jobs = [], []
-    for i in range(n):
-        N, S = int(specs["side"][i]), int(specs["S"][i])
-        pu, pv = dp.ptrs(N, int(specs["set"][i]), int(specs["offset"][i]))
-        o = torch.empty(N * N, dtype=torch.complex64, device=dev)
-        outs.append(o)
-        j = gg.gg_job()
-        j.out, j.uv, j.vals, j.gcf = o.data_ptr(), pu, pv, dg[S].data_ptr()
-        j.npts, j.img_dim, j.gcf_dim = int(specs["nvis"][i]), N, S
-        j.uv_type, j.vals_type, j.out_type = gg.C128, gg.C64, gg.C64
-        jobs.append(j)
+    jobs, outs, _ = stream_jobs(js, n, dev)
     ctx = gg.Context(local_rank)
     plan = gg.Plan(ctx, opts, jobs)
     s = torch.cuda.Stream()
@@ -820,7 +769,7 @@ def run_batch(args, rank, world, local_rank, dist):
     launches = per_step * args.steps
     # accuracy on a sample of jobs
     sample = list(range(0, n, max(1, n // 12)))[:12]
-    acc = check_sample([outs[i].cpu().numpy() for i in sample], pools, specs, gcfs, sample) \
+    acc = check_sample([outs[i].cpu().numpy() for i in sample], js, sample) \
         if rank == 0 and not args.no_check else None
     # plain per-job launches
     plain = {}
@@ -851,8 +800,16 @@ def run_batch(args, rank, world, local_rank, dist):
     # e2e through the server's host path: one batch of host requests
     e2e = None
     if not args.no_e2e:
-        hp = {N: (torch.from_numpy(uv).pin_memory().numpy(), torch.from_numpy(v).pin_memory().numpy())
-              for N, (uv, v) in pools.items()}
+        h_uv = torch.empty((total_vis, 2), dtype=torch.float64).pin_memory()
+        h_v = torch.empty(total_vis, dtype=torch.complex64).pin_memory()
+        hoff, o = [], 0
+        for i in range(n):
+            uvd, vd = js.device_job(i)
+            h_uv[o:o + len(uvd)].copy_(uvd)
+            h_v[o:o + len(vd)].copy_(vd)
+            hoff.append(o)
+            o += len(uvd)
+        torch.cuda.synchronize()
         houts = [torch.empty(int(N) * int(N), dtype=torch.complex64).pin_memory().numpy()
                  for N in specs["side"]]
         # host path: 3 stream slots, batches of up to 64 jobs, so that copies of
@@ -861,12 +818,9 @@ def run_batch(args, rank, world, local_rank, dist):
         gids = {S: srv.add_gcf(gcfs[S]) for S in (8, 16)}
         reqs = []
         for i in range(n):
-            N, S = int(specs["side"][i]), int(specs["S"][i])
-            s_, off, nv_ = int(specs["set"][i]), int(specs["offset"][i]), int(specs["nvis"][i])
-            uvh, vh = hp[N]
-            L = uvh.shape[1]
-            reqs.append(gg.Server.request(uvh.ctypes.data + (s_ * L + off) * 16,
-                                          vh.ctypes.data + (s_ * L + off) * 8,
+            N, S, nv_ = js.shape(i)
+            reqs.append(gg.Server.request(h_uv.data_ptr() + hoff[i] * 16,
+                                          h_v.data_ptr() + hoff[i] * 8,
                                           houts[i].ctypes.data, nv_, N, S, gids[S]))
         zeros = np.zeros(n)
         for _ in range(2):
@@ -1234,7 +1188,7 @@ def run_reference(args, rank, world):
     # cpu_baseline of the GPU arm's line
     jobs, desc = cpu_sample(w)
     desc_n = (w["npts"] if w["kind"] == "single"
-              else int(stream_inputs(w["n"], seed=stream_seed(w["kind"]))[1]["nvis"].sum()))
+              else JobStream(w["n"], stream_seed(w["kind"])).total_vis())
 
     def step():
         _, vis, t, _ = cpu_rate(jobs, threads)

@@ -119,44 +119,60 @@ def tile_sort(uv: np.ndarray, img_dim: int, tile: int = 32, gcf_dim: int = 8,
     return np.argsort(key, kind="stable")
 
 
-def track_pool(sides=(256, 512, 1024, 2048), nsets: int = 8, seed: int = 0,
-               nant: int = 64, ntime: int = 2080):
-    """Per grid side, `nsets` independent observations with the track
-    geometry of the 4096^2 workload (nant antennas at random positions in a
-    2 km disk, all baselines, ntime hour-angle samples over +-4 h at dec -30
-    deg, 90% fill), each a different antenna layout: {side: (uv[nsets, nbl *
-    ntime, 2] float64, vals[nsets, nbl * ntime] complex64)}, baseline-major.
-    Jobs of the batched and served workloads are contiguous slices of these
-    (whole baseline tracks at the full time sampling)."""
-    pools = {}
-    for i, N in enumerate(sides):
-        uvs, vs = [], []
-        for s in range(nsets):
-            uv, v = tracks(N, nant=nant, ntime=ntime, npts=None,
-                           seed=seed * 1000 + i * 100 + s)
-            uvs.append(uv)
-            vs.append(v)
-        pools[N] = (np.stack(uvs), np.stack(vs))
-    return pools
+def job_tracks(img_dim: int, nvis: int, seed: int, device="cpu", nant: int = 64,
+               ntime: int = 2080, ha_hours: float = 4.0, dec_deg: float = -30.0,
+               fill: float = 0.9, radius_m: float = 1000.0):
+    """One request's own observation (the batched and served workloads): an
+    array of nant antennas at random positions in a disk of radius_m -- its
+    own layout, drawn from `seed` -- of which ceil(nvis / ntime) baselines,
+    picked at random, are tracked over ntime hour angles in [-ha, ha] at
+    declination dec_deg; (u, v) in pixels centred at img_dim / 2, scaled so
+    that the array's longest baseline spans fill * img_dim / 2 (the largest
+    |u|, |v| any of its tracks can reach); float-representable coordinates;
+    complex64 N(0, 1) values.  Baseline-major, time-minor, cut to nvis.
+    Computed with torch on `device` (the layout and the baseline choice on
+    the host from `seed`, the values from a generator of `device` seeded
+    with it).  Returns (uv float64 (nvis, 2), vals complex64 (nvis,))
+    tensors on `device`."""
+    import torch
+    g = torch.Generator().manual_seed(int(seed))
+    r = radius_m * torch.sqrt(torch.rand(nant, generator=g, dtype=torch.float64))
+    th = 2 * math.pi * torch.rand(nant, generator=g, dtype=torch.float64)
+    ax, ay = r * torch.cos(th), r * torch.sin(th)
+    i, j = torch.triu_indices(nant, nant, 1)
+    bx, by = ax[j] - ax[i], ay[j] - ay[i]
+    lmax = float(torch.sqrt(bx * bx + by * by).max())
+    nbl = min(bx.numel(), -(-int(nvis) // ntime))
+    pick = torch.randperm(bx.numel(), generator=g)[:nbl]
+    bx, by = bx[pick].to(device), by[pick].to(device)
+    ha = torch.linspace(-ha_hours, ha_hours, ntime, dtype=torch.float64,
+                        device=device) * (math.pi / 12.0)
+    sd = math.sin(math.radians(dec_deg))
+    sh, ch = torch.sin(ha)[None, :], torch.cos(ha)[None, :]
+    u = sh * bx[:, None] + ch * by[:, None]
+    v = -sd * ch * bx[:, None] + sd * sh * by[:, None]
+    scale = fill * (img_dim / 2) / lmax
+    uv = torch.stack([img_dim / 2 + u.reshape(-1) * scale,
+                      img_dim / 2 + v.reshape(-1) * scale], dim=1)[:nvis]
+    uv = uv.float().double().contiguous()
+    gd = torch.Generator(device=device).manual_seed(int(seed))
+    vals = torch.randn(int(nvis), 2, generator=gd, device=device, dtype=torch.float32)
+    return uv, torch.view_as_complex(vals.contiguous())
 
 
 def request_specs(n: int, seed: int = 0, sides=(256, 512, 1024, 2048),
                   supports=(8, 16), nvis_min: float = 1e4, nvis_max: float = 1e6,
-                  log10_mean: float = 5.0, log10_sd: float = 0.5,
-                  nsets: int = 8, pool_len: int = 2016 * 2080):
+                  log10_mean: float = 5.0, log10_sd: float = 0.5):
     """Job / request shapes of the batched and served workloads: grid side
     uniform over `sides`, support uniform over `supports`, visibility count
     lognormal (log10 ~ N(log10_mean, log10_sd)) clipped to [nvis_min,
-    nvis_max], and a random slice of one pool track set."""
+    nvis_max].  Each job's visibilities come from job_tracks."""
     rng = np.random.default_rng(seed)
     side = rng.choice(np.asarray(sides), n)
     S = rng.choice(np.asarray(supports), n)
     nvis = np.clip(10.0 ** rng.normal(log10_mean, log10_sd, n), nvis_min,
                    nvis_max).astype(np.int64)
-    tset = rng.integers(0, nsets, n)
-    off = (rng.random(n) * (pool_len - nvis + 1)).astype(np.int64)
-    return {"side": side.astype(np.int64), "S": S.astype(np.int64), "nvis": nvis,
-            "set": tset.astype(np.int64), "offset": off}
+    return {"side": side.astype(np.int64), "S": S.astype(np.int64), "nvis": nvis}
 
 
 def gaussian_gcf_1d(gcf_dim: int, oversample: int = 8,
