@@ -384,6 +384,67 @@ class JobStream:
         return sum(uv.numel() * 8 + v.numel() * 8 for uv, v in self.dev.values())
 
 
+ACC_NOTE = ("max_rel / rms_rel: normwise, |gpu - oracle| / max |oracle| (max) and "
+            "||gpu - oracle|| / ||oracle|| (rms) over the grid; cell_max / cell_rms: per "
+            "cell, |gpu - oracle| / sum |v||w| of the cell's additions (forward error of "
+            "each cell's sum), over the cells that receive any")
+
+
+class ErrAcc:
+    """normwise and per-cell error of grids against the FP64 oracle,
+    accumulated over several grids (planar (2, P, N, N) float64 each)"""
+
+    def __init__(self):
+        self.worst = self.num = self.den = 0.0
+        self.cmax = self.csq = 0.0
+        self.cells = 0
+
+    def add(self, got, ref, mag):
+        self.worst = max(self.worst, float(np.abs(got - ref).max() /
+                                           max(np.abs(ref).max(), 1e-300)))
+        self.num += float(((got - ref) ** 2).sum())
+        self.den += float((ref ** 2).sum())
+        d = np.hypot(got[0] - ref[0], got[1] - ref[1])
+        hit = mag > 0
+        if np.any(d[~hit] != 0):
+            self.cmax = float("inf")
+        e = d[hit] / mag[hit]
+        if e.size:
+            self.cmax = max(self.cmax, float(e.max()))
+            self.csq += float((e * e).sum())
+            self.cells += int(e.size)
+
+    def result(self, **extra):
+        r = {"max_rel": self.worst, "rms_rel": (self.num / max(self.den, 1e-300)) ** 0.5,
+             "cell_max": self.cmax,
+             "cell_rms": (self.csq / max(self.cells, 1)) ** 0.5}
+        r.update(extra)
+        r["reference"] = "FP64 oracle (gridCPU_pz restatement)"
+        return r
+
+
+def oracle_pair(uv, vals, gcf, N, S):
+    """(planar FP64 grid, per-cell magnitude sums) of the oracle"""
+    import oracle as O
+    t = os.cpu_count() or 1
+    return (O.grid_pz(uv, pairs(vals), pairs(gcf), N, S, nthreads=t),
+            O.grid_mag(uv, pairs(vals), pairs(gcf), N, S, nthreads=t))
+
+
+def window_reference(uv, vals, gcf, N, S, x0, y0, B):
+    """Oracle of the B x B window [x0, x0+B) x [y0, y0+B) of an N^2 grid:
+    every visibility whose footprint can reach the window, shifted by an
+    integer offset (exact in FP64 and keeping u, v float-representable, so
+    main and oversample indices shift exactly) onto a (B + 2S)^2 grid.
+    Returns (ref, mag) of the window, planar (2, 1, B, B) and (1, B, B)."""
+    m = np.floor(uv)
+    keep = ((m[:, 0] >= x0 - S) & (m[:, 0] < x0 + B + S) &
+            (m[:, 1] >= y0 - S) & (m[:, 1] < y0 + B + S))
+    sub = uv[keep] - np.array([x0 - S, y0 - S], np.float64)
+    ref, mag = oracle_pair(sub, vals[keep], gcf, B + 2 * S, S)
+    return ref[:, :, S:S + B, S:S + B], mag[:, S:S + B, S:S + B], int(keep.sum())
+
+
 def check_sample(grids, st, idx):
     """normwise and per-cell error of device grids vs the FP64 oracle"""
     acc = ErrAcc()
