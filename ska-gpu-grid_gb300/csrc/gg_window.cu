@@ -17,7 +17,10 @@
 //    For each residue it keeps a register sum while the target cell stays the
 //    same and, when it changes, adds the sum into the sub-grid.  Ownership
 //    makes that read-modify-write exclusive: no atomics, and no
-//    synchronisation between visibilities.
+//    synchronisation between visibilities.  One-warp groups, whose lanes
+//    step through the records together, own taps instead on interior tiles
+//    (fixed table offsets, a __syncwarp per run), which halves the table's
+//    L1 footprint.
 //  * FP32 sums are compensated: sub-grid cells hold a (hi, lo) pair per
 //    component, updated with Knuth's TwoSum on the packed (re, im) pair
 //    (f32x2 instructions) whenever a register run is added in; register runs
@@ -266,6 +269,16 @@ __global__ void __launch_bounds__(kWinThreads, win_min_ctas(S, W, MODE))
   }
   const int nitems = *kp.nitems;
   const bool leader = gt == 0;
+  // One-warp groups on interior tiles own taps instead of residues: thread
+  // gt adds the taps (rx, ry[k]) of every footprint, so its table offsets are
+  // the same for every record -- only the first S rows of each row-doubled
+  // sub-kernel are read, half the L1 footprint of the rotating offsets (for
+  // support 16, 64 KB instead of 128 KB beside two CTAs' sub-grids) -- and
+  // its cells move with the footprint.  A cell then passes from lane to lane
+  // across footprint moves, ordered by __syncwarp.  Wider groups, whose
+  // warps run apart, keep residue ownership (no cell shared by threads).
+  // Each cell still receives the same register sums in the same order.
+  constexpr bool TAPS = W == 1 && S * S % NGT == 0;
 
   if (leader) {
     mbar_init(&bar[0], 1);
@@ -483,12 +496,13 @@ __global__ void __launch_bounds__(kWinThreads, win_min_ctas(S, W, MODE))
           VT2 va = vb[r], vb1, vc1;
           const int fx0 = (int)((unsigned)pk.x & 0xffffu) - kWinMainBias - H + 1;
           const int fy0 = (int)((unsigned)pk.x >> 16) - kWinMainBias - H + 1;
+          if constexpr (TAPS) __syncwarp();  // other lanes' cell updates seen
           if (MODE == 1 && run >= kRunMax) flush_runs();
           if (fx0 != pfx || fy0 != pfy) {
             pfx = fx0;
             pfy = fy0;
-            pax = (rx - fx0) & (S - 1);
-            const int b0 = (ry[0] - fy0) & (S - 1);
+            pax = TAPS ? rx : (rx - fx0) & (S - 1);
+            const int b0 = TAPS ? ry[0] : (ry[0] - fy0) & (S - 1);
             pofs = GAUSS ? b0 : b0 * S + pax;
             const int lx = fx0 + pax - ox;
             if constexpr (S * S % NGT == 0) {
@@ -615,6 +629,7 @@ __global__ void __launch_bounds__(kWinThreads, win_min_ctas(S, W, MODE))
       if (leader) issue_next(g + 3);
     }
     if (s_abort[gid]) break;
+    if constexpr (TAPS) __syncwarp();
 #pragma unroll
     for (int k = 0; k < Q; ++k)
       if (cur[k] >= 0) {
