@@ -1348,7 +1348,7 @@ def main():
     ap.add_argument("--method", choices=["scatter", "gather", "window"], default=None,
                     help="single-job workloads: grid with this method instead of the "
                          "workload's own")
-    ap.add_argument("--e2e-ring", type=int, default=64,
+    ap.add_argument("--e2e-ring", type=int, default=256,
                     help="served10k e2e: pinned host output buffers per grid side that the "
                          "client cycles through (requests in flight <= 4 x this)")
     ap.add_argument("--profile-batch", action="store_true",

@@ -277,6 +277,7 @@ struct gg_context {
   std::mutex mu;
   DevBuf ws;        // plan workspace
   DevBuf flags;     // int32[16]: flags[0..7], item counters [8..11], item_next [12..15]
+  int *batch_flags = nullptr;  // set by the server: the flag words of its batch
   HostBuf staging;  // pinned: device tables are uploaded from here
   cudaEvent_t upload_done = nullptr;  // staging may be rewritten after this
   cudaEvent_t exec_done = nullptr;    // workspace free after this
@@ -291,7 +292,10 @@ struct gg_context {
   cudaEvent_t prof[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
-int *gg::context_flags(gg_context *c) { return (int *)c->flags.p; }
+int *gg::context_flags(gg_context *c) {
+  return c->batch_flags ? c->batch_flags : (int *)c->flags.p;
+}
+void gg::context_set_batch_flags(gg_context *c, int *flags) { c->batch_flags = flags; }
 
 static int ctx_init(gg_context *c, int device) {
   c->device = device;
@@ -786,10 +790,12 @@ struct ProfEvents {
 };
 
 // Enqueue the whole computation on stream s: zeroing, binning, work queue,
-// gridding kernels.  `upload` (pinned host tables) is copied into the
-// workspace first when given, and `upload_ev` recorded right after that copy
-// (the staging buffer is free again from there on, so the host can prepare
-// the next call while this one runs); a plan whose tables are already
+// gridding kernels.  `upload` (host tables) is sent into the workspace first
+// when given, through kernel parameters (launch_upload): a copy-engine
+// transfer would queue behind other streams' input and output copies (one
+// to two milliseconds per batch on a server moving host data), a launch does
+// not, and the staging buffer is free again when the call returns
+// (`upload_ev` is still recorded after it); a plan whose tables are already
 // resident passes null, and then nothing here reads host memory, allocates
 // or synchronises -- the sequence can be captured into a CUDA graph.
 static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int sm_count,
@@ -798,7 +804,7 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
   char *ws = pl.ws;
   if (prof) GG_CUDA(cudaEventRecord(prof->ev[0], s));
   if (upload) {
-    GG_CUDA(cudaMemcpyAsync(ws, upload, pl.table_bytes, cudaMemcpyHostToDevice, s));
+    GG_CUDA(launch_upload(ws, upload, pl.table_bytes, s));
     if (upload_ev) GG_CUDA(cudaEventRecord(upload_ev, s));
   }
   const JobDesc *djobs = (const JobDesc *)(ws + pl.o_jobs);
@@ -975,7 +981,7 @@ static int enqueue_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs
   GG_CUDA(cudaStreamWaitEvent(s, c->exec_done, 0));
   ProfEvents pe;
   for (int i = 0; i < 4; ++i) pe.ev[i] = c->prof[i];
-  st = plan_enqueue(opt, pl, (int *)c->flags.p, c->sm_count, s, c->staging.p,
+  st = plan_enqueue(opt, pl, gg::context_flags(c), c->sm_count, s, c->staging.p,
                     c->upload_done, c->profile ? &pe : nullptr, &c->aux);
   if (st) return st;
   if (c->profile) c->prof_recorded = 1;
@@ -1511,7 +1517,7 @@ int gg_bin(gg_context *ctx, const gg_options *opt, int uv_type, const void *uv,
   char *ws = (char *)ctx->ws.p;
   cudaStream_t s = (cudaStream_t)stream;
   GG_CUDA(cudaStreamWaitEvent(s, ctx->exec_done, 0));
-  GG_CUDA(cudaMemcpyAsync(ws, ctx->staging.p, pl.table_bytes, cudaMemcpyHostToDevice, s));
+  GG_CUDA(launch_upload(ws, ctx->staging.p, pl.table_bytes, s));
   GG_CUDA(cudaEventRecord(ctx->upload_done, s));
   BinBuffers b{};
   b.jobs = (const BinJob *)(ws + pl.o_bin);

@@ -13,7 +13,9 @@
 //
 // All kernels work on a batch of jobs sharing one global visibility index
 // space and one global tile space; a single job is a batch of one.
+#include <algorithm>
 #include <climits>
+#include <cstring>
 
 #include "gg_kernels.cuh"
 
@@ -513,6 +515,36 @@ __global__ void inject_flags_kernel(int *flags, int bits) {
 cudaError_t launch_inject_flags(int *flags, int bits, cudaStream_t s) {
   inject_flags_kernel<<<1, 1, 0, s>>>(flags, bits);
   count_launch();
+  return cudaGetLastError();
+}
+
+// ---- table upload through kernel parameters -------------------------------------
+// A launch carries its parameters with it (copied by the driver at the call),
+// so tables sent this way never wait on a copy engine behind the bulk
+// transfers of other streams, and the host buffer is free once the call
+// returns.
+constexpr int kUploadChunk = 16384;  // bytes per launch (parameters: up to 32 KB)
+struct UploadChunk {
+  uint4 *dst;
+  int n16;  // 16-byte words in this chunk
+  uint4 data[kUploadChunk / 16];
+};
+
+__global__ void __launch_bounds__(256) upload_kernel(const __grid_constant__ UploadChunk p) {
+  for (int i = threadIdx.x; i < p.n16; i += 256) p.dst[i] = p.data[i];
+}
+
+cudaError_t launch_upload(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+  if (bytes % 16 || (uintptr_t)dst % 16) return cudaErrorInvalidValue;
+  static thread_local UploadChunk p;  // 16 KB: off the stack
+  for (size_t o = 0; o < bytes; o += kUploadChunk) {
+    const size_t n = std::min<size_t>(kUploadChunk, bytes - o);
+    p.dst = reinterpret_cast<uint4 *>(static_cast<char *>(dst) + o);
+    p.n16 = (int)(n / 16);
+    memcpy(p.data, static_cast<const char *>(src) + o, n);
+    upload_kernel<<<1, 256, 0, s>>>(p);
+    count_launch();
+  }
   return cudaGetLastError();
 }
 

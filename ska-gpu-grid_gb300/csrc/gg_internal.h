@@ -121,8 +121,17 @@ cudaError_t launch_merge_finalize(const MergeSlots &m, const int *heavy_counter,
 // ORs `bits` (1 << FLAG_*) into flags[FLAG_*] on the stream: the host-side
 // injection behind gg_debug_inject_device_flags.
 cudaError_t launch_inject_flags(int *flags, int bits, cudaStream_t s);
+// Copies `bytes` (a multiple of 16, dst 16-byte aligned) from host memory to
+// dst on the stream through kernel parameters, 16 KB per launch: nothing
+// waits on a copy engine, and src may be rewritten once the call returns.
+cudaError_t launch_upload(void *dst, const void *src, size_t bytes, cudaStream_t s);
 // flags of a context (device int32[64], see gg_read_flags)
 int *context_flags(gg_context *c);
+// Makes the batched calls of a context use `flags` (device int32[64], the
+// caller zeroes words 0..7) instead of its own flag words, until reset with
+// null: the request server gives every batch in flight its own words, read
+// back after the batch's output copies while the slot runs its next batch.
+void context_set_batch_flags(gg_context *c, int *flags);
 // consumes one pending injection of gg_debug_inject_device_flags: returns
 // its bits (0: none pending)
 int injected_device_flags();

@@ -9,13 +9,23 @@
 //    order, up to the batch limits) is staged and gridded there in ONE
 //    batched launch (gg_grid_batch: one binning pass and one persistent
 //    window kernel per support over all of them);
+//  * a batch is a three-stage pipeline: its input copies on the server's
+//    input stream, its kernels on the slot's stream (waiting on an event),
+//    its output copies and the read-back of its device flag words on the
+//    server's output stream (waiting on an event behind the kernels).  The
+//    slot takes its next batch as soon as the kernels finish, so host-bound
+//    traffic keeps both directions of the host link busy;
+//  * every batch in flight has its own device flag words (an entry of a
+//    ring; the slot's context is pointed at it for the batch), so a slot's
+//    next batch cannot clear flags not yet read back;
 //  * staging uses stream-ordered allocation (cudaMallocAsync from the
 //    device's memory pool) so that a batch allocates nothing synchronously;
-//    inputs and host-bound grids are freed in stream order after the copies;
-//  * completion is signalled by a host function enqueued behind the batch
-//    (cudaLaunchHostFunc), which only flags the slot and wakes the
-//    scheduler; the scheduler finishes the requests, returns their budget
-//    and wakes waiters;
+//    inputs are freed behind the kernels, host-bound grids behind their
+//    copies;
+//  * host functions enqueued behind the kernels and behind the output stage
+//    (cudaLaunchHostFunc) only flag the slot / the batch and wake the
+//    scheduler, which frees slots, finishes requests in launch order,
+//    returns their budget and wakes waiters;
 //  * latency is measured from a request's arrival (its submit time, or its
 //    scheduled time in a trace) to that completion.
 #include <algorithm>
@@ -54,18 +64,33 @@ struct Req {
   cudaStream_t stream = nullptr;
 };
 
+// A slot = one gg_context (its own workspace) + one stream for the kernels
+// of its current batch.  It is free again as soon as those kernels finish;
+// the batch's output copies run on the server's output stream.
 struct Slot {
   cudaStream_t s = nullptr;
   gg_context *ctx = nullptr;
-  // pinned copy of the batch's device flag words, read back behind the
-  // batch's kernels and checked when the batch completes
-  int32_t *hflags = nullptr;
-  std::vector<Req *> batch;
-  bool busy = false;
-  bool done = false;
-  int64_t seq = 0;  // batches the server launched before this one
+  std::vector<Req *> batch;  // being admitted
+  bool busy = false;         // its batch's kernels are queued or running
+  bool free_again = false;   // set by the host function behind those kernels
+  int64_t seq = 0;           // batches the server launched before this one
   struct gg_server *srv = nullptr;
 };
+
+// A batch from its launch until its requests complete (its output copies and
+// the read-back of its device flag words have finished).
+struct Batch {
+  std::vector<Req *> reqs;
+  int ring = -1;  // entry of the server's flag-word ring used by its kernels
+  cudaEvent_t ev_in = nullptr, ev_compute = nullptr;
+  int launch_status = GG_OK;
+  bool done = false;  // set by the host function behind the output stage
+  struct gg_server *srv = nullptr;
+};
+
+// flag-word ring: one entry (int32[64], the words a context's batched calls
+// use) per batch in flight; the scheduler launches nothing while it is full
+constexpr int kFlagRing = 1024;
 
 int elem(int type) { return type == GG_C128 ? 16 : 8; }
 
@@ -82,6 +107,18 @@ struct gg_server {
   int64_t used = 0, peak = 0;
   bool stop = false;
   std::vector<std::unique_ptr<Slot>> slots;
+  // Pipeline: the input copies of every batch go on s_in, its kernels on its
+  // slot's stream, its output copies on s_out, ordered by events.  One
+  // stream per direction keeps each copy engine fed in launch order, and a
+  // slot starts its next batch while earlier grids are still being copied
+  // out (a slot kept until its copies end ran in lock-step with the others,
+  // the output link idle 40 % of the time).
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  int *d_ring = nullptr;      // kFlagRing x 64 int32 (device)
+  int32_t *h_ring = nullptr;  // kFlagRing x 4 int32 (pinned): words 0..3 read back
+  std::vector<int> ring_free;
+  std::vector<cudaEvent_t> ev_free;
+  std::vector<std::unique_ptr<Batch>> inflight;  // launch order
   std::vector<void *> gcf_ptr;
   std::vector<int64_t> gcf_dim;
   std::vector<int> gcf_type;
@@ -109,12 +146,32 @@ struct gg_server {
 
 namespace {
 
-void on_batch_done(void *p) {
+// host functions (no CUDA calls): flag the event and wake the scheduler
+void on_slot_free(void *p) {
   Slot *slot = static_cast<Slot *>(p);
   gg_server *srv = slot->srv;
   std::lock_guard<std::mutex> lk(srv->mu);
-  slot->done = true;
+  slot->free_again = true;
   srv->cv_sched.notify_one();
+}
+
+void on_batch_done(void *p) {
+  Batch *b = static_cast<Batch *>(p);
+  gg_server *srv = b->srv;
+  std::lock_guard<std::mutex> lk(srv->mu);
+  b->done = true;
+  srv->cv_sched.notify_one();
+}
+
+cudaEvent_t take_event(gg_server *srv) {
+  if (!srv->ev_free.empty()) {
+    cudaEvent_t e = srv->ev_free.back();
+    srv->ev_free.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+  return e;
 }
 
 // bytes a request holds on the device while admitted
@@ -162,12 +219,12 @@ int validate(const gg_server *srv, const gg_request &r) {
   return GG_OK;
 }
 
-void finish_batch(gg_server *srv, Slot *slot) {
+void finish_batch(gg_server *srv, Batch *b) {
   const double t = srv->now();
   // device flags of the batch: a timeout, unsorted input or a failed bounds
   // check fails every request of the batch (its grids are incomplete);
   // dropped visibilities are reported and the requests succeed
-  const int32_t *h = slot->hflags;
+  const int32_t *h = srv->h_ring + 4 * b->ring;
   const int bits = (h[gg::FLAG_INDEX] ? GG_DEVFLAG_INDEX : 0) |
                    (h[gg::FLAG_TIMEOUT] ? GG_DEVFLAG_TIMEOUT : 0) |
                    (h[gg::FLAG_UNSORTED] ? GG_DEVFLAG_UNSORTED : 0) |
@@ -176,12 +233,12 @@ void finish_batch(gg_server *srv, Slot *slot) {
                          : h[gg::FLAG_UNSORTED] ? GG_ERR_UNSORTED
                          : h[gg::FLAG_BOUNDS]   ? GG_ERR_STATE
                                                 : GG_OK;
-  for (Req *q : slot->batch) {
+  for (Req *q : b->reqs) {
     q->device_flags = bits;
     if (q->state == R_LAUNCHED && q->status == GG_OK && dev_status != GG_OK) {
       q->status = dev_status;
       if (q->own_out && q->d_out) {  // a resident grid of a failed request
-        cudaFreeAsync(q->d_out, slot->s);
+        cudaFreeAsync(q->d_out, srv->s_out);
         q->own_out = false;
         q->d_out = nullptr;
       }
@@ -202,23 +259,27 @@ void finish_batch(gg_server *srv, Slot *slot) {
     q->bytes = q->resident_bytes;
   }
   srv->last_done = t;
-  slot->batch.clear();
-  slot->busy = false;
-  slot->done = false;
+  srv->ring_free.push_back(b->ring);
+  if (b->ev_in) srv->ev_free.push_back(b->ev_in);
+  if (b->ev_compute) srv->ev_free.push_back(b->ev_compute);
   srv->cv_done.notify_all();
 }
 
-// Stage and launch one batch on a slot (called without the lock).
-void launch_batch(gg_server *srv, Slot *slot) {
+// Stage and launch one batch on a slot (called without the lock): input
+// copies on s_in, zeroing / binning / kernels on the slot's stream, output
+// copies and the flag read-back on s_out.
+void launch_batch(gg_server *srv, Slot *slot, Batch *b) {
   cudaSetDevice(srv->cfg.device);
-  cudaStream_t s = slot->s;
+  cudaStream_t s = slot->s, si = srv->s_in, so = srv->s_out;
+  int *dflags = srv->d_ring + (size_t)64 * b->ring;
   std::vector<gg_job> jobs;
-  jobs.reserve(slot->batch.size());
+  jobs.reserve(b->reqs.size());
   int st = GG_OK;
+  bool any_in = false;
   const int64_t P = srv->cfg.options.polarizations;
-  for (Req *q : slot->batch) {
+  for (Req *q : b->reqs) {
     const gg_request &r = q->r;
-    q->stream = s;
+    q->stream = so;
     cudaError_t e = cudaSuccess;
     if (r.flags & GG_REQ_INPUTS_ON_DEVICE) {
       q->d_uv = const_cast<void *>(r.uv);
@@ -227,16 +288,17 @@ void launch_batch(gg_server *srv, Slot *slot) {
       const size_t bu = (size_t)r.npts * elem(r.uv_type);
       const size_t bv = (size_t)r.npts * elem(r.vals_type) * P;
       e = gg::injected_alloc_failure() ? cudaErrorMemoryAllocation
-                                       : cudaMallocAsync(&q->d_uv, bu, s);
+                                       : cudaMallocAsync(&q->d_uv, bu, si);
       if (e == cudaSuccess) {
         q->own_uv = true;
-        e = cudaMallocAsync(&q->d_vals, bv, s);
+        e = cudaMallocAsync(&q->d_vals, bv, si);
       }
       if (e == cudaSuccess) {
         q->own_vals = true;
-        e = cudaMemcpyAsync(q->d_uv, r.uv, bu, cudaMemcpyHostToDevice, s);
+        any_in = true;
+        e = cudaMemcpyAsync(q->d_uv, r.uv, bu, cudaMemcpyHostToDevice, si);
       }
-      if (e == cudaSuccess) e = cudaMemcpyAsync(q->d_vals, r.vals, bv, cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(q->d_vals, r.vals, bv, cudaMemcpyHostToDevice, si);
     }
     if (e == cudaSuccess) {
       if (r.flags & GG_REQ_OUT_ON_DEVICE) {
@@ -268,44 +330,62 @@ void launch_batch(gg_server *srv, Slot *slot) {
     j.out_type = r.out_type;
     jobs.push_back(j);
   }
+  if (any_in && (cudaEventRecord(b->ev_in, si) != cudaSuccess ||
+                 cudaStreamWaitEvent(s, b->ev_in, 0) != cudaSuccess) &&
+      st == GG_OK)
+    st = GG_ERR_CUDA;
   // autotuner trials (which synchronise the slot's stream) only while the
   // server is young; afterwards the cached choices are reused
   gg_options opt = srv->cfg.options;
   if (opt.autotune == 1 && slot->seq >= GG_SERVER_TUNE_BATCHES) opt.autotune = 2;
-  int *dflags = gg::context_flags(slot->ctx);
-  for (int i = 0; i < 4; ++i) slot->hflags[i] = 0;
-  if (st == GG_OK && cudaMemsetAsync(dflags, 0, 4 * sizeof(int), s) != cudaSuccess)
+  if (st == GG_OK && cudaMemsetAsync(dflags, 0, 64 * sizeof(int), s) != cudaSuccess)
     st = GG_ERR_CUDA;
-  if (st == GG_OK) st = gg_grid_batch(slot->ctx, &opt, jobs.data(), (int32_t)jobs.size(), s);
+  if (st == GG_OK) {
+    gg::context_set_batch_flags(slot->ctx, dflags);
+    st = gg_grid_batch(slot->ctx, &opt, jobs.data(), (int32_t)jobs.size(), s);
+    gg::context_set_batch_flags(slot->ctx, nullptr);
+  }
   if (st == GG_OK) {
     if (const int inj = gg::injected_device_flags())
       if (gg::launch_inject_flags(dflags, inj, s) != cudaSuccess) st = GG_ERR_CUDA;
   }
-  if (st == GG_OK &&
-      cudaMemcpyAsync(slot->hflags, dflags, 4 * sizeof(int), cudaMemcpyDeviceToHost, s) !=
-          cudaSuccess)
-    st = GG_ERR_CUDA;
-  for (Req *q : slot->batch) {
+  // inputs are read by this batch's kernels only
+  for (Req *q : b->reqs) {
+    if (q->own_uv) cudaFreeAsync(q->d_uv, s);
+    if (q->own_vals) cudaFreeAsync(q->d_vals, s);
+    q->own_uv = q->own_vals = false;
+    q->d_uv = q->d_vals = nullptr;
+  }
+  if (cudaEventRecord(b->ev_compute, s) != cudaSuccess && st == GG_OK) st = GG_ERR_CUDA;
+  if (cudaLaunchHostFunc(s, on_slot_free, slot) != cudaSuccess) {
+    cudaStreamSynchronize(s);  // no callback: free the slot synchronously
+    on_slot_free(slot);
+  }
+  // output stage, behind the kernels
+  cudaStreamWaitEvent(so, b->ev_compute, 0);
+  for (Req *q : b->reqs) {
     if (st != GG_OK && q->status == GG_OK) q->status = st;
     const gg_request &r = q->r;
     const bool host_out = !(r.flags & (GG_REQ_OUT_ON_DEVICE | GG_REQ_KEEP_RESIDENT));
     if (st == GG_OK && host_out && q->d_out)
       cudaMemcpyAsync(r.out, q->d_out, (size_t)elem(r.out_type) * P * r.img_dim * r.img_dim,
-                      cudaMemcpyDeviceToHost, s);
-    if (q->own_uv) cudaFreeAsync(q->d_uv, s);
-    if (q->own_vals) cudaFreeAsync(q->d_vals, s);
-    q->own_uv = q->own_vals = false;
-    q->d_uv = q->d_vals = nullptr;
+                      cudaMemcpyDeviceToHost, so);
     if (q->own_out && (host_out || st != GG_OK)) {
-      cudaFreeAsync(q->d_out, s);
+      cudaFreeAsync(q->d_out, so);
       q->own_out = false;
       q->d_out = nullptr;
     }
   }
-  if (cudaLaunchHostFunc(s, on_batch_done, slot) != cudaSuccess) {
-    // no callback: finish synchronously
-    cudaStreamSynchronize(s);
-    on_batch_done(slot);
+  if (st == GG_OK && cudaMemcpyAsync(srv->h_ring + 4 * b->ring, dflags, 4 * sizeof(int32_t),
+                                     cudaMemcpyDeviceToHost, so) != cudaSuccess) {
+    st = GG_ERR_CUDA;
+    for (Req *q : b->reqs)
+      if (q->status == GG_OK) q->status = st;
+  }
+  b->launch_status = st;
+  if (cudaLaunchHostFunc(so, on_batch_done, b) != cudaSuccess) {
+    cudaStreamSynchronize(so);
+    on_batch_done(b);
   }
 }
 
@@ -314,14 +394,22 @@ void scheduler(gg_server *srv) {
   std::unique_lock<std::mutex> lk(srv->mu);
   for (;;) {
     for (auto &sl : srv->slots)
-      if (sl->busy && sl->done) finish_batch(srv, sl.get());
+      if (sl->busy && sl->free_again) {
+        sl->busy = false;
+        sl->free_again = false;
+      }
+    // batches complete in launch order (one output stream)
+    while (!srv->inflight.empty() && srv->inflight.front()->done) {
+      finish_batch(srv, srv->inflight.front().get());
+      srv->inflight.erase(srv->inflight.begin());
+    }
     Slot *free_slot = nullptr;
     for (auto &sl : srv->slots)
       if (!sl->busy) {
         free_slot = sl.get();
         break;
       }
-    if (free_slot && !srv->pending.empty()) {
+    if (free_slot && !srv->pending.empty() && !srv->ring_free.empty()) {
       // admit in arrival order while the budget and batch limits allow
       int64_t vis = 0;
       while (!srv->pending.empty() &&
@@ -344,18 +432,35 @@ void scheduler(gg_server *srv) {
         free_slot->batch.push_back(q);
       }
       if (!free_slot->batch.empty()) {
+        std::unique_ptr<Batch> nb(new Batch);
+        Batch *b = nb.get();
+        b->srv = srv;
+        b->reqs.swap(free_slot->batch);
+        b->ring = srv->ring_free.back();
+        srv->ring_free.pop_back();
+        for (int i = 0; i < 4; ++i) srv->h_ring[4 * b->ring + i] = 0;
+        b->ev_in = take_event(srv);
+        b->ev_compute = take_event(srv);
+        srv->inflight.push_back(std::move(nb));
         free_slot->busy = true;
-        free_slot->done = false;
+        free_slot->free_again = false;
         free_slot->seq = srv->n_launched++;
         ++srv->n_batches;
-        srv->n_batch_jobs += (int64_t)free_slot->batch.size();
+        srv->n_batch_jobs += (int64_t)b->reqs.size();
+        if (!b->ev_in || !b->ev_compute) {
+          // no events: fail the batch without launching anything
+          for (Req *q : b->reqs) q->status = GG_ERR_CUDA;
+          free_slot->busy = false;
+          b->done = true;
+          continue;
+        }
         lk.unlock();
-        launch_batch(srv, free_slot);
+        launch_batch(srv, free_slot, b);
         lk.lock();
         continue;
       }
     }
-    bool any_busy = false;
+    bool any_busy = !srv->inflight.empty();
     for (auto &sl : srv->slots) any_busy |= sl->busy;
     if (srv->stop && srv->pending.empty() && !any_busy && srv->feeders_running == 0) break;
     srv->cv_sched.wait(lk);
@@ -406,32 +511,44 @@ int gg_server_create(gg_server **out, const gg_server_config *cfg) {
     uint64_t keep = ~0ull;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
+  // everything made so far is released on a failure below
+  auto undo = [&]() {
+    for (auto &x : srv->slots) {
+      gg_destroy(x->ctx);
+      cudaStreamDestroy(x->s);
+    }
+    srv->slots.clear();
+    if (srv->s_in) cudaStreamDestroy(srv->s_in);
+    if (srv->s_out) cudaStreamDestroy(srv->s_out);
+    if (srv->d_ring) cudaFree(srv->d_ring);
+    if (srv->h_ring) cudaFreeHost(srv->h_ring);
+  };
   for (int i = 0; i < cfg->streams; ++i) {
     std::unique_ptr<Slot> sl(new Slot);
     sl->srv = srv.get();
     int st = gg_create(&sl->ctx, cfg->device);
     if (st) {
-      for (auto &x : srv->slots) {
-        gg_destroy(x->ctx);
-        cudaStreamDestroy(x->s);
-        cudaFreeHost(x->hflags);
-      }
+      undo();
       return st;
     }
-    cudaStreamCreateWithFlags(&sl->s, cudaStreamNonBlocking);
-    if (cudaMallocHost(&sl->hflags, 4 * sizeof(int32_t)) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&sl->s, cudaStreamNonBlocking) != cudaSuccess) {
       gg_destroy(sl->ctx);
-      cudaStreamDestroy(sl->s);
-      for (auto &x : srv->slots) {
-        gg_destroy(x->ctx);
-        cudaStreamDestroy(x->s);
-        cudaFreeHost(x->hflags);
-      }
-      return set_error(GG_ERR_NOMEM, "server: pinned flag words");
+      undo();
+      return set_error(GG_ERR_CUDA, "server: stream");
     }
-    for (int i = 0; i < 4; ++i) sl->hflags[i] = 0;
     srv->slots.push_back(std::move(sl));
   }
+  if (cudaStreamCreateWithFlags(&srv->s_in, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&srv->s_out, cudaStreamNonBlocking) != cudaSuccess) {
+    undo();
+    return set_error(GG_ERR_CUDA, "server: copy streams");
+  }
+  if (cudaMalloc(&srv->d_ring, sizeof(int) * 64 * kFlagRing) != cudaSuccess ||
+      cudaMallocHost(&srv->h_ring, sizeof(int32_t) * 4 * kFlagRing) != cudaSuccess) {
+    undo();
+    return set_error(GG_ERR_NOMEM, "server: flag words");
+  }
+  for (int i = kFlagRing - 1; i >= 0; --i) srv->ring_free.push_back(i);
   gg_server *p = srv.release();
   p->sched = std::thread(scheduler, p);
   *out = p;
@@ -654,7 +771,7 @@ int gg_server_drain(gg_server *srv, double timeout_s) {
   if (!srv) return set_error(GG_ERR_ARG, "server: null");
   std::unique_lock<std::mutex> lk(srv->mu);
   auto idle = [srv] {
-    if (!srv->pending.empty() || srv->feeders_running) return false;
+    if (!srv->pending.empty() || srv->feeders_running || !srv->inflight.empty()) return false;
     for (auto &sl : srv->slots)
       if (sl->busy) return false;
     return true;
@@ -689,13 +806,23 @@ int gg_server_destroy(gg_server *srv) {
   srv->sched.join();
   cudaSetDevice(srv->cfg.device);
   for (auto &sl : srv->slots) cudaStreamSynchronize(sl->s);
+  cudaStreamSynchronize(srv->s_in);
+  cudaStreamSynchronize(srv->s_out);
   for (auto &kv : srv->reqs)
     if (kv.second->own_out && kv.second->d_out) cudaFree(kv.second->d_out);
   cudaDeviceSynchronize();
   for (auto &sl : srv->slots) {
     gg_destroy(sl->ctx);
     cudaStreamDestroy(sl->s);
-    cudaFreeHost(sl->hflags);
+  }
+  cudaStreamDestroy(srv->s_in);
+  cudaStreamDestroy(srv->s_out);
+  cudaFree(srv->d_ring);
+  cudaFreeHost(srv->h_ring);
+  for (cudaEvent_t e : srv->ev_free) cudaEventDestroy(e);
+  for (auto &b : srv->inflight) {
+    if (b->ev_in) cudaEventDestroy(b->ev_in);
+    if (b->ev_compute) cudaEventDestroy(b->ev_compute);
   }
   for (void *p : srv->gcf_ptr) cudaFree(p);
   delete srv;

@@ -179,10 +179,11 @@ __host__ __device__ constexpr int win_default_warps(int S, int T) {
 template <int S, int W> struct WinCfg {
   static constexpr int NGT = 32 * W;                         // threads per group
   static constexpr int Q = (S * S + NGT - 1) / NGT;          // residues per thread
-  // records per chunk (staging buffers); 64 for S=16 lets three CTAs' shared
-  // memory (3 x 70 KB) fit an SM, which measured faster than two CTAs with
-  // more L1 left for the GCF table
-  static constexpr int K = S >= 32 ? 512 : (S >= 16 ? 64 : 128);
+  // records per chunk (staging buffers).  48 for S=16: two CTAs of one-warp
+  // groups on 8-cell tiles then take 159.5 KB of shared memory, under the
+  // 164 KB carveout, which leaves 92 KB of L1 for the 64 KB of table rows the
+  // tap-owning lanes read (64 records per chunk left 60 KB: 5 % slower)
+  static constexpr int K = S >= 32 ? 512 : (S >= 16 ? 48 : 128);
   static constexpr int GROUPS = kWinThreads / NGT;
 
 };
