@@ -59,8 +59,10 @@ STREAM_DESC = ("grid side uniform in {256,512,1024,2048}; support 8 or 16, "
                "tracks4096 geometry: its own 64 antennas at random positions in "
                "a 2 km disk, whole tracks of a random choice of its 2016 "
                "baselines, 2080 samples over +-4 h, dec -30 deg, the longest "
-               "baseline at 90% fill; complex64 N(0,1) values; FP64 "
-               "u,v; complex64 grids; FP32 compensated accumulation; "
+               "baseline at 90% fill; complex64 N(0,1) values; FP32 "
+               "u,v (float2, as the reference's FP32 instantiation "
+               "gridGPU<float2,float2> takes them); complex64 grids; FP32 "
+               "compensated accumulation; "
                "tabulated separable Gaussian GCFs resident on the device")
 
 WORKLOADS = {
@@ -73,12 +75,13 @@ WORKLOADS = {
                           "launch captured in a CUDA graph: " + STREAM_DESC),
     "tracks4096": dict(
         kind="single", N=4096, S=8, npts=1 << 22, gen="tracks", vals="c64", out="c64",
-        mode="auto", accum="comp", presort=True,
+        uv="f32", mode="auto", accum="comp", presort=True,
         desc=("4096^2 complex64 grid; 2^22 visibilities on uv tracks (64 "
               "antennas in a 2 km disk, 2016 baselines x 2080 hour angles over "
               "+-4 h at dec -30 deg, 90% fill, +1024 to 2^22); complex64 N(0,1) "
-              "values; FP64 u,v; support 8, oversample 8; presorted into 32x32 "
-              "uv tiles; FP32 compensated accumulation")),
+              "values; FP32 u,v (float2, as gridGPU<float2,float2> takes them); "
+              "support 8, oversample 8; presorted into 32x32 uv tiles; FP32 "
+              "compensated accumulation")),
     "uniform1024": dict(
         kind="single", N=1024, S=16, npts=1 << 18, gen="uniform", vals="c128", out="c128",
         mode="scatter", accum="plain",
@@ -361,11 +364,14 @@ class JobStream:
         return int(self.specs["nvis"][: self.n if n is None else n].sum())
 
     def device_job(self, i):
-        """(uv float64 (n, 2), vals complex64 (n,)) tensors on the device"""
+        """(uv float32 (n, 2), vals complex64 (n,)) tensors on the device; the
+        coordinates are generated float-representable, so the float32 copy
+        is exact"""
         if i not in self.dev:
             import synth
             N, _, n = self.shape(i)
-            self.dev[i] = synth.job_tracks(N, n, self.seed * 100003 + i, self.device)
+            uv, v = synth.job_tracks(N, n, self.seed * 100003 + i, self.device)
+            self.dev[i] = (uv.float().contiguous(), v)
         return self.dev[i]
 
     def generate(self, n=None):
@@ -381,7 +387,7 @@ class JobStream:
         return uv.cpu().numpy(), v.cpu().numpy()
 
     def device_bytes(self):
-        return sum(uv.numel() * 8 + v.numel() * 8 for uv, v in self.dev.values())
+        return sum(uv.numel() * 4 + v.numel() * 8 for uv, v in self.dev.values())
 
 
 ACC_NOTE = ("max_rel / rms_rel: normwise, |gpu - oracle| / max |oracle| (max) and "
@@ -471,7 +477,7 @@ def stream_jobs(st, n, dev):
         j = gg.gg_job()
         j.out, j.uv, j.vals, j.gcf = grids[-1].data_ptr(), pu, pv, dg[S].data_ptr()
         j.npts, j.img_dim, j.gcf_dim = nv, N, S
-        j.uv_type, j.vals_type, j.out_type = gg.C128, gg.C64, gg.C64
+        j.uv_type, j.vals_type, j.out_type = gg.C64, gg.C64, gg.C64
         jobs.append(j)
     return jobs, grids, dg
 
@@ -537,7 +543,8 @@ def run_served(args, rank, world, local_rank, dist):
     for i in range(n):
         N, S, nv = js.shape(i)
         pu, pv = js.ptrs(i)
-        reqs.append(gg.Server.request(pu, pv, None, nv, N, S, gids[S], flags=flags))
+        reqs.append(gg.Server.request(pu, pv, None, nv, N, S, gids[S], flags=flags,
+                                      uv_type=gg.C64))
 
     def stream(offsets, keep=()):
         """submit all requests at the given arrival offsets; wait, release;
@@ -620,7 +627,7 @@ def run_served(args, rank, world, local_rank, dist):
             j = gg.gg_job()
             j.out, j.uv, j.vals, j.gcf = outs[N].data_ptr(), pu, pv, dg[S].data_ptr()
             j.npts, j.img_dim, j.gcf_dim = nv, N, S
-            j.uv_type, j.vals_type, j.out_type = gg.C128, gg.C64, gg.C64
+            j.uv_type, j.vals_type, j.out_type = gg.C64, gg.C64, gg.C64
             jobs.append(j)
         for j in jobs[:50]:
             ctx.grid_job(o, j)
@@ -658,7 +665,7 @@ def run_served(args, rank, world, local_rank, dist):
         import torch as _t
         # every request's inputs in pinned host memory (copied once from the
         # generated device inputs, outside the timed passes)
-        h_uv = _t.empty((total_vis, 2), dtype=_t.float64).pin_memory()
+        h_uv = _t.empty((total_vis, 2), dtype=_t.float32).pin_memory()
         h_v = _t.empty(total_vis, dtype=_t.complex64).pin_memory()
         hoff, o = [], 0
         for i in range(n):
@@ -679,9 +686,10 @@ def run_served(args, rank, world, local_rank, dist):
             b = used[N] % RING
             used[N] += 1
             hbuf.append((N, b))
-            hreqs.append(gg.Server.request(h_uv.data_ptr() + hoff[i] * 16,
+            hreqs.append(gg.Server.request(h_uv.data_ptr() + hoff[i] * 8,
                                            h_v.data_ptr() + hoff[i] * 8,
-                                           hout[N][b].data_ptr(), nv_, N, S, gids[S], flags=0))
+                                           hout[N][b].data_ptr(), nv_, N, S, gids[S], flags=0,
+                                           uv_type=gg.C64))
 
         def host_pass():
             owner = {}                       # (side, buffer) -> ticket using it
@@ -722,7 +730,7 @@ def run_served(args, rank, world, local_rank, dist):
             assert acc_h["max_rel"] < 1e-6, acc_h
         t_all = max_over_ranks(t_all, dist, dev)
         e2e = {"value": round(replica_rate(total_vis * reps, world, t_all), 3), "unit": "Mvis/s",
-               "h2d_bytes_per_step": int(total_vis * 24),
+               "h2d_bytes_per_step": int(total_vis * 16),
                "d2h_bytes_per_step": int(sum(8 * int(N) * int(N) for N in specs["side"])),
                "ms_per_step": round(1e3 * t_all / reps, 3),
                "api": "gg_server_* (C ABI): host requests, inputs copied in from pinned "
@@ -861,7 +869,7 @@ def run_batch(args, rank, world, local_rank, dist):
     # e2e through the server's host path: one batch of host requests
     e2e = None
     if not args.no_e2e:
-        h_uv = torch.empty((total_vis, 2), dtype=torch.float64).pin_memory()
+        h_uv = torch.empty((total_vis, 2), dtype=torch.float32).pin_memory()
         h_v = torch.empty(total_vis, dtype=torch.complex64).pin_memory()
         hoff, o = [], 0
         for i in range(n):
@@ -880,9 +888,10 @@ def run_batch(args, rank, world, local_rank, dist):
         reqs = []
         for i in range(n):
             N, S, nv_ = js.shape(i)
-            reqs.append(gg.Server.request(h_uv.data_ptr() + hoff[i] * 16,
+            reqs.append(gg.Server.request(h_uv.data_ptr() + hoff[i] * 8,
                                           h_v.data_ptr() + hoff[i] * 8,
-                                          houts[i].ctypes.data, nv_, N, S, gids[S]))
+                                          houts[i].ctypes.data, nv_, N, S, gids[S],
+                                          uv_type=gg.C64))
         zeros = np.zeros(n)
         for _ in range(2):
             for t in srv.submit_schedule(reqs, zeros):
@@ -898,7 +907,7 @@ def run_batch(args, rank, world, local_rank, dist):
         srv.close()
         t_all = max_over_ranks(t_all, dist, dev)
         e2e = {"value": round(replica_rate(total_vis * reps, world, t_all), 3), "unit": "Mvis/s",
-               "h2d_bytes_per_step": int(total_vis * 24),
+               "h2d_bytes_per_step": int(total_vis * 16),
                "d2h_bytes_per_step": int(sum(8 * int(N) * int(N) for N in specs["side"])),
                "ms_per_step": round(1e3 * t_all / reps, 3),
                "api": "gg_server_* (C ABI) with host input and output buffers (3 stream "
@@ -973,7 +982,10 @@ def run_single(args, rank, world, local_rank, dist):
     uv, vals, gcf = make_single(w, seed=1000 + rank)
     o = single_options(w)
     odt = torch.complex64 if w["out"] == "c64" else torch.complex128
-    d_uv = torch.from_numpy(uv).to(dev)
+    # float2 coordinates for the FP32 workloads (exact: generated
+    # float-representable); the oracle reads the same values in FP64
+    uv_in = uv.astype(np.float32) if w.get("uv") == "f32" else uv
+    d_uv = torch.from_numpy(uv_in).to(dev)
     d_vals = torch.from_numpy(vals).to(dev)
     d_gcf = torch.from_numpy(gcf.reshape(-1)).to(dev)
     out = torch.empty(N * N, dtype=odt, device=dev)
@@ -1047,7 +1059,8 @@ def run_single(args, rank, world, local_rank, dist):
     total_ms = max_over_ranks(total_ms, dist, dev)
     e2e = None
     if not args.no_e2e:
-        pin_uv = torch.from_numpy(uv.view(np.complex128).reshape(-1)).pin_memory().numpy()
+        cuv = uv_in.view(np.complex64 if uv_in.dtype == np.float32 else np.complex128)
+        pin_uv = torch.from_numpy(cuv.reshape(-1)).pin_memory().numpy()
         pin_vals = torch.from_numpy(vals).pin_memory().numpy()
         pin_gcf = torch.from_numpy(gcf.reshape(-1)).pin_memory().numpy()
         pin_out = torch.zeros(gg.padded_size(N, S), dtype=odt).pin_memory().numpy()
