@@ -238,6 +238,38 @@ def test_autotune_lookup_only_never_times(ctx):
     assert relerr(got, grid_alone(ctx, OPTS, N, S, uv, vals, GCF[S])) <= TOL
 
 
+def test_server_pipeline_keeps_flags_with_their_batch(ctx):
+    """The server pipelines batches (input copies, kernels on a slot, output
+    copies on a shared stream) and gives every batch in flight its own device
+    flag words.  Twelve host requests, one per batch, submitted at once over
+    two slots: a flag raised on the first three batches (from the host,
+    behind their kernels) reaches exactly those requests while later batches
+    run on the same slots, and every grid equals the request gridded alone."""
+    rng = np.random.default_rng(8)
+    data = [make_request_data(800 + k, rng) for k in range(12)]
+    with gg.Server(streams=2, max_batch_jobs=1, options=OPTS) as srv:
+        gids = {S: srv.add_gcf(GCF[S]) for S in (8, 16)}
+        outs, reqs = [], []
+        for N, S, uv, vals in data:
+            outs.append(np.full(N * N, np.nan, np.complex64))
+            reqs.append(gg.Server.request(uv.ctypes.data, vals.ctypes.data,
+                                          outs[-1].ctypes.data, len(uv), N, S, gids[S]))
+        gg.inject_device_flags(gg.DEVFLAG_INDEX, 3)
+        try:
+            tickets = srv.submit_schedule(reqs, np.zeros(len(reqs)))
+            res = [srv.wait(int(t), timeout=120) for t in tickets]
+        finally:
+            gg.inject_device_flags(0, 0)
+        for t in tickets:
+            srv.release(int(t))
+        assert [r.device_flags for r in res] == [gg.DEVFLAG_INDEX] * 3 + [0] * 9
+        assert all(r.status == gg.OK for r in res)
+        for (N, S, uv, vals), out in zip(data, outs):
+            assert relerr(out, grid_alone(ctx, OPTS, N, S, uv, vals, GCF[S])) <= TOL
+        st = srv.stats()
+        assert st["completed"] == 12 and st["batches"] == 12 and st["hbm_in_use"] == 0
+
+
 def test_server_reports_device_flags(ctx):
     """Device-side failures reach the requests of their batch: the server
     reads the batch's flag words back behind its kernels.  A bounded-wait
