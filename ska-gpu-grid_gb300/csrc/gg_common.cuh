@@ -26,9 +26,14 @@ namespace gg {
 // same conversions so that main and sub are bit-exact with the CPU gridder
 // for every finite u.  For float-representable u the result also equals the
 // GPU driver's all-double formula (grid_gpu.cu:118-121, 358-363).
-// The step for float coordinates with |u| < 2^23, entirely in FP32:
-// floorf(u) is exact, u - floorf(u) is exact and so is the power-of-two scale,
-// so this equals the double formula below on (double)u.
+// The step for float coordinates with |u| < 2^23, entirely in FP32.
+// floorf(u) is exact, and so is u - floorf(u) except for -1/2 < u < 0, where
+// 1 + u rounds to float exactly as the CPU gridder's double difference does
+// when its product with the power of two G is converted to float (the scale
+// commutes with the rounding; 1 + u may even round to 1, an oversample index
+// of G, which the binning drops and counts).  So this equals the double
+// formula below on (double)u.  (floor(G*u) in one conversion gives the same
+// integers outside (-1/2, 0) and measured no faster in the binning pass.)
 __device__ __forceinline__ void index_step_f32(float u, int G, int &m, int &s) {
   float fl = floorf(u);
   s = (int)floorf(__fmul_rn((float)G, __fsub_rn(u, fl)));

@@ -162,6 +162,37 @@ def test_vis2ints_bit_exact_fp32(ctx):
     assert np.array_equal(got, O.vis2ints(uv32.astype(np.float64)))
 
 
+def test_vis2ints_bit_exact_near_zero_and_half(ctx):
+    """The FP32 index step where u - floorf(u) rounds (-1/2 < u < 0) and
+    around it: values on both sides of -1/2, -1/4, -1/8, 0 and -1, tiny
+    negatives whose 1 + u rounds to 1 (oversample index G), negative
+    multiples of 1/G and signed zeros, as float and as float-representable
+    double coordinates, bit-exact with the oracle."""
+    rng = np.random.default_rng(12)
+    f32 = np.float32
+    special = [0.0, -0.0, -1e-30, -1e-10, -2.0 ** -25, -2.0 ** -24, -0.5, -1.0, -1.5, 0.5,
+               -0.125, -0.375, -0.625, -0.875, -0.25, -2.0 ** -149 * 1e30]
+    near = []
+    for x in (-0.5, -0.25, -0.125, -1.0, -2.0, 0.0, 0.125):
+        v = f32(x)
+        for _ in range(4):
+            v = np.nextafter(v, f32(-np.inf))
+            near.append(v)
+        v = f32(x)
+        for _ in range(4):
+            v = np.nextafter(v, f32(np.inf))
+            near.append(v)
+    dense = rng.uniform(-1.0, 0.0, 100000).astype(f32)
+    mult = -(np.arange(1, 800, dtype=f32) / f32(8)) + rng.choice([-1, 0, 1], 799).astype(f32) * f32(2.0 ** -26)
+    vals = np.concatenate([np.array(special, f32), np.array(near, f32), dense, mult.astype(f32)])
+    uv32 = np.stack([vals, vals[::-1]], -1).astype(f32)
+    ref = O.vis2ints(uv32.astype(np.float64))
+    got32 = gg.vis2ints(torch.from_numpy(np.ascontiguousarray(uv32)).cuda()).cpu().numpy()
+    assert np.array_equal(got32, ref)
+    got64 = gg.vis2ints(torch.from_numpy(uv32.astype(np.float64)).cuda()).cpu().numpy()
+    assert np.array_equal(got64, ref)
+
+
 @pytest.mark.parametrize("T", [8, 32])
 @pytest.mark.parametrize("input_sorted", [False, True])
 def test_bin_bookmarks(ctx, input_sorted, T):
