@@ -107,7 +107,15 @@ typedef struct gg_options {
                             made so far (the nearest size class of the same
                             support and arithmetic; defaults when there is
                             none) and never time trials.                   */
-  int32_t reserved[5];
+  int32_t accumulate;    /* 1: add the gridded values into the present
+                            contents of each job's `out` instead of
+                            overwriting it (device entry points: summing
+                            w-planes, facets or snapshots into one grid; the
+                            host entry points always overwrite).  Autotuner
+                            trials, which write the outputs, are not run:
+                            choices made so far are reused as with
+                            autotune = 2.                                    */
+  int32_t reserved[4];
 } gg_options;
 
 /* Defaults = the reference built with no Makefile switches: SCATTER,

@@ -186,6 +186,8 @@ static int check_options(const gg_options *o) {
     return fail(GG_ERR_ARG, "options: group_warps %d not in {0,1,2,4,8}", o->group_warps);
   if (o->autotune < 0 || o->autotune > 2)
     return fail(GG_ERR_ARG, "options: autotune %d not in {0,1,2}", o->autotune);
+  if (o->accumulate != 0 && o->accumulate != 1)
+    return fail(GG_ERR_ARG, "options: accumulate %d not in {0,1}", o->accumulate);
   return GG_OK;
 }
 
@@ -722,7 +724,9 @@ static int plan_build(gg_context *c, const gg_options *opt, const gg_job *jobs,
     pl.htile_base[k] = tb;
     pl.hclass[k] = (int)pl.classes.size() - 1;
     const size_t out_bytes = (size_t)(D.out_f64 ? 16 : 8) * pl.P * N * N;
-    if (mode != GG_MODE_GATHER) pl.zero_ranges.push_back({J.out, out_bytes});
+    // the binned scatter-type kernels add into the grid: cleared first unless
+    // the caller accumulates into it (gather stores, or adds, every cell)
+    if (mode != GG_MODE_GATHER && !opt->accumulate) pl.zero_ranges.push_back({J.out, out_bytes});
     if (pl.comp_lo && J.out_type == GG_C64) {
       // filled in once the workspace base is known (plan_bind)
       D.lo = reinterpret_cast<float *>(lo_off + 1);
@@ -862,6 +866,7 @@ static int plan_enqueue(const gg_options *opt, const Plan &pl, int *flags, int s
   g.G = pl.G;
   g.tile = pl.T;
   g.group_warps = pl.group_warps;
+  g.accumulate = opt->accumulate;
   g.P = pl.P;
   g.flags = flags;
   g.sm_count = sm_count;
@@ -997,7 +1002,9 @@ static int enqueue_jobs(gg_context *c, const gg_options *opt, const gg_job *jobs
 // launch then overwrites; they synchronise stream s.
 static int autotune_batch(gg_context *c, const gg_options *opt, const gg_job *jobs, int njobs,
                           cudaStream_t s) {
-  if (opt->autotune != 1 || !tunable(opt) || njobs < 1 || !jobs) return GG_OK;
+  // trials write the outputs: none when the caller accumulates into them
+  if (opt->autotune != 1 || opt->accumulate || !tunable(opt) || njobs < 1 || !jobs)
+    return GG_OK;
   int maxS = 0;
   for (int j = 0; j < njobs; ++j) maxS = std::max<int>(maxS, (int)jobs[j].gcf_dim);
   if (resolve_mode(opt, maxS, jobs[0].vals_type == GG_C128) != GG_MODE_WINDOW) return GG_OK;
@@ -1616,7 +1623,9 @@ extern "C" int gg_grid_host(const gg_options *opt, int out_type, void *out,
   j.uv_type = uv_type;
   j.vals_type = vals_type;
   j.out_type = out_type;
-  st = grid_jobs(c, opt, &j, 1, s);
+  gg_options ho = *opt;
+  ho.accumulate = 0;  // the device copy of the grid starts empty: overwrite
+  st = grid_jobs(c, &ho, &j, 1, s);
   if (st) return st;
   char *o = (char *)out;
   GG_CUDA(cudaMemcpyAsync(o + ob * head, c->h_out.p, ob * grid_elems, cudaMemcpyDeviceToHost, s));

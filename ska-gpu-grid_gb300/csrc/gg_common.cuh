@@ -260,6 +260,18 @@ __device__ __forceinline__ void grid_red<double>(double *out, size_t cell, int p
   }
 }
 
+// one finished cell added to the grid's present value (gather into a grid it
+// accumulates into): the sum formed in FP64, rounded once to the grid's type
+template <typename OT>
+__device__ __forceinline__ void grid_add(OT *out, size_t cell, int p, int P, size_t NN,
+                                         bool planar, double re, double im) {
+  const size_t c = (size_t)p * NN + cell;
+  OT *a = planar ? out + c : out + 2 * c;
+  OT *b = planar ? out + (size_t)P * NN + c : out + 2 * c + 1;
+  *a = (OT)((double)*a + re);
+  *b = (OT)((double)*b + im);
+}
+
 // plain store of one finished cell (gather writes every cell exactly once)
 template <typename OT>
 __device__ __forceinline__ void grid_store(OT *out, size_t cell, int p, int P,

@@ -274,10 +274,16 @@ __global__ void __launch_bounds__(kGatherThreads)
             fre = acc[k].fre();
             fim = acc[k].fim();
           }
-          if (J.out_f64)
+          if (kp.accumulate) {  // into the present value, rounded once
+            if (J.out_f64)
+              grid_add<double>((double *)J.out, cell, p, P, NN, J.planar, dre, dim);
+            else
+              grid_add<float>((float *)J.out, cell, p, P, NN, J.planar, dre, dim);
+          } else if (J.out_f64) {
             grid_store<double>((double *)J.out, cell, p, P, NN, J.planar, dre, dim);
-          else
+          } else {
             grid_store<float>((float *)J.out, cell, p, P, NN, J.planar, fre, fim);
+          }
         }
       }
     }
@@ -335,6 +341,7 @@ cudaError_t launch_gather(const GridLaunch &g, cudaStream_t s) {
   kp.T = g.tile;
   kp.G = g.G;
   kp.sigma = g.sigma;
+  kp.accumulate = g.accumulate;
   switch (g.S) {
     case 4: return gather_dispatch<4>(g, kp, s);
     case 8: return gather_dispatch<8>(g, kp, s);

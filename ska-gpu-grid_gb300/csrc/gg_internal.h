@@ -152,6 +152,7 @@ struct GridLaunch {
   int G;                   // oversampling, uniform over the launch
   int tile;                // uv tile side, uniform over the launch
   int group_warps;         // moving window: warps per sub-grid (0: by support)
+  int accumulate;          // gather: add into the grid instead of storing
   int P;
   int *flags;
   const int *holes;        // binned methods: bookmarks[total_tiles + 1]

@@ -24,6 +24,7 @@ struct KParams {
   int T;        // uv tile side, uniform within a launch
   int G;        // oversampling, uniform within a launch
   float sigma;  // GAUSS sigma, uniform within a launch
+  int accumulate;  // gather: add each finished cell into the grid
   // moving window, compensated FP32 into complex64 grids: FP64 merge slots
   // of the tiles cut into several work items (base null: none)
   MergeSlots merge;

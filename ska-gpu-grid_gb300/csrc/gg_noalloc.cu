@@ -267,7 +267,7 @@ extern "C" int gg_grid_device_noalloc(const gg_options *opt, const gg_job *job,
   GG_NA(cudaGetLastError());
   int *flags = (int *)(ws + kOffFlags);
   const size_t out_bytes = (size_t)(D.out_f64 ? 16 : 8) * N * N;
-  GG_NA(cudaMemsetAsync(job->out, 0, out_bytes, s));
+  if (!opt->accumulate) GG_NA(cudaMemsetAsync(job->out, 0, out_bytes, s));
 
   if (opt->gcf_kind == GG_GCF_TABLE)
     GG_NA(launch_gcf_double_rows(job->gcf, ws + kOffGcf, (int)S, G, 1, 8, s));

@@ -57,7 +57,8 @@ class gg_options(ctypes.Structure):
                 ("window_chunk", ctypes.c_int32),
                 ("group_warps", ctypes.c_int32),
                 ("autotune", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 5)]
+                ("accumulate", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 4)]
 
 
 class gg_job(ctypes.Structure):
@@ -198,6 +199,7 @@ class Options:
     group_warps: int = 0                # moving window: warps per sub-grid
     autotune: int = 0                   # moving window: tile / warps / chunk by timing
                                         # (1: time new size classes, 2: reuse choices)
+    accumulate: bool = False            # device entry points: add into `out`
 
     def c(self) -> gg_options:
         o = gg_options()
@@ -209,6 +211,7 @@ class Options:
         o.gcf_sigma, o.window_chunk = self.gcf_sigma, self.window_chunk
         o.group_warps = self.group_warps
         o.autotune = int(self.autotune)
+        o.accumulate = int(bool(self.accumulate))
         return o
 
 

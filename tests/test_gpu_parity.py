@@ -668,3 +668,61 @@ def test_window_support_32_four_warp_groups(ctx, prec, T):
     out, flags = run(ctx, o, uv, vals, gcf, N, S, prec)
     assert flags == [0, 0, 0, 0]
     check(out, prec, uv, vals, gcf, N, S)
+
+
+# ---------------------------------------------------------------------------
+# accumulate: add into the present grid (device entry points)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("layout", [gg.LAYOUT_INTERLEAVED, gg.LAYOUT_PLANAR])
+@pytest.mark.parametrize("prec", ["zz", "cc_comp"])
+@pytest.mark.parametrize("mode", ["scatter", "gather", "window"])
+def test_accumulate_adds_into_the_present_grid(ctx, mode, prec, layout):
+    """options.accumulate = 1: the gridded values are added to what `out`
+    holds (a random grid here, in the layout's own memory order), for every
+    method, FP64 and compensated FP32, both layouts, two polarisations; the
+    autotuner does not run (its trials would write the outputs)."""
+    N, S, P = 128, 8, 2
+    uv, vals = synth.tracks(N, nant=16, ntime=200, npts=30000, seed=31)
+    rng = np.random.default_rng(32)
+    vals = (rng.standard_normal(len(uv) * P) + 1j * rng.standard_normal(len(uv) * P))
+    vdt = np.complex128 if prec == "zz" else np.complex64
+    vals = vals.astype(vdt)
+    gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(vdt)
+    odt = torch.complex128 if prec == "zz" else torch.complex64
+    o = opts_for(mode, prec, layout=layout, polarizations=P, accumulate=True, autotune=1)
+    base = (rng.standard_normal(P * N * N) + 1j * rng.standard_normal(P * N * N))
+    out = torch.from_numpy(base.astype(np.complex128)).to(odt).cuda()
+    start = torch.view_as_real(out).reshape(-1).cpu().numpy().copy()
+    ctx.grid(o, out, torch.from_numpy(uv).cuda(), torch.from_numpy(vals).cuda(),
+             torch.from_numpy(gcf.reshape(-1)).cuda(), N, S)
+    torch.cuda.synchronize()
+    assert ctx.read_flags() == [0, 0, 0, 0]
+    planar = layout == gg.LAYOUT_PLANAR
+    got = planar_from_grid(torch.view_as_real(out).reshape(-1).cpu().numpy(), P, N, planar)
+    ref = oracle_for(uv, vals, gcf, N, S, P=P) + planar_from_grid(start, P, N, planar)
+    assert rel_err(got, ref) <= (1e-12 if prec == "zz" else 1e-6)
+
+
+def test_accumulate_batch_twice_is_two_grids(ctx):
+    """A batched window call with accumulate = 1 run twice into the same
+    (zeroed) outputs gives twice the grid of each job."""
+    jobs, keep, refs = [], [], []
+    for k, (N, S) in enumerate([(128, 8), (256, 16), (64, 8)]):
+        uv, vals = synth.tracks(N, nant=12, ntime=150, npts=20000, seed=40 + k)
+        gcf = synth.gcf_table(synth.gaussian_gcf_1d(S)).astype(np.complex64)
+        d = [torch.from_numpy(uv).cuda(), torch.from_numpy(vals).cuda(),
+             torch.from_numpy(gcf.reshape(-1)).cuda(),
+             torch.zeros(N * N, dtype=torch.complex64, device="cuda")]
+        keep.append(d)
+        jobs.append(gg.Context.make_job(d[3], d[0], d[1], d[2], N, S))
+        refs.append(2.0 * oracle_for(uv, vals, gcf, N, S))
+    o = gg.Options(mode=gg.MODE_WINDOW, accum=gg.ACC_COMPENSATED,
+                   layout=gg.LAYOUT_INTERLEAVED, accumulate=True)
+    ctx.grid_batch(o, jobs)
+    ctx.grid_batch(o, jobs)
+    torch.cuda.synchronize()
+    assert ctx.read_flags() == [0, 0, 0, 0]
+    for d, ref, j in zip(keep, refs, jobs):
+        N = j.img_dim
+        got = planar_from_grid(torch.view_as_real(d[3]).reshape(-1).cpu().numpy(), 1, N, False)
+        assert rel_err(got, ref) <= 1e-6
