@@ -111,7 +111,8 @@ typedef struct gg_options {
                             contents of each job's `out` instead of
                             overwriting it (device entry points: summing
                             w-planes, facets or snapshots into one grid; the
-                            host entry points always overwrite).  Autotuner
+                            host entry points and the request server always
+                            overwrite).  Autotuner
                             trials, which write the outputs, are not run:
                             choices made so far are reused as with
                             autotune = 2.                                    */

@@ -338,6 +338,7 @@ void launch_batch(gg_server *srv, Slot *slot, Batch *b) {
   // server is young; afterwards the cached choices are reused
   gg_options opt = srv->cfg.options;
   if (opt.autotune == 1 && slot->seq >= GG_SERVER_TUNE_BATCHES) opt.autotune = 2;
+  opt.accumulate = 0;  // every request gets a fresh grid
   if (st == GG_OK && cudaMemsetAsync(dflags, 0, 64 * sizeof(int), s) != cudaSuccess)
     st = GG_ERR_CUDA;
   if (st == GG_OK) {
