@@ -310,6 +310,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                "r"(bytes)
                : "memory");
 }
+// one arrival (no transaction bytes), e.g. a consumer releasing a buffer
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 // src, dst 16-byte aligned; bytes a multiple of 16
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
                                          uint32_t bytes, uint64_t *bar) {

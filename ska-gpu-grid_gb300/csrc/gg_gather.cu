@@ -9,8 +9,12 @@
 // memory by 1-D TMA bulk copies, and every warp compacts, with ballots, the
 // records of a chunk whose footprint overlaps its own band into a list of its
 // own -- a footprint of S rows reaches about S/4 + 1 of the 8 bands, and a
-// warp never visits the records that miss it.  Warps synchronise only once
-// per chunk (before its buffer is refilled).
+// warp never visits the records that miss it.  The chunks of a tile's 9 bins
+// (and of the CTA's next planes and tiles) form one stream through
+// kGatherStages buffers with a full and an empty mbarrier each: a buffer is
+// refilled once every warp has released it, so the warps of a tile drift
+// apart by a few chunks (track segments give the row bands unequal shares)
+// instead of meeting at a barrier after every chunk.
 // Each output cell is then written exactly once with a plain store: no
 // atomics, no pre-zeroed grid, and a fixed summation order per cell.
 #include <type_traits>
@@ -28,14 +32,18 @@ constexpr int kGatherRun = 32;
 constexpr int kGatherTile = 32;
 constexpr int kGatherThreads = 256;
 
+// chunk buffers in flight per CTA
+constexpr int kGatherStages = 4;
+
 template <typename VT2>
 struct GatherShape {
+  static constexpr int HEAD = 16 * kGatherStages;  // full and empty mbarriers
   static constexpr int IDX_BUF = kGatherChunk * 8 + 16;
   static constexpr int VAL_BUF = kGatherChunk * (int)sizeof(VT2) + 16;
   // per-warp lists of record indices (16 bits: a chunk has at most 512)
   static constexpr int LIST_BYTES = (kGatherThreads / 32) * kGatherChunk * 2;
   static constexpr size_t smem(int S) {
-    return 16 + 2 * IDX_BUF + 2 * VAL_BUF + LIST_BYTES + 64 * S * 4;
+    return HEAD + kGatherStages * (IDX_BUF + VAL_BUF) + LIST_BYTES + 64 * S * 4;
   }
 };
 
@@ -61,27 +69,41 @@ __global__ void __launch_bounds__(kGatherThreads)
   // call fails with GG_ERR_UNSORTED -- grid nothing
   if (kp.holes && *kp.holes) return;
   extern __shared__ __align__(16) unsigned char smem[];
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-  // double buffers, addressed arithmetically (buffer b at +b*size)
-  unsigned char *const idx0 = smem + 16;
-  unsigned char *const val0 = smem + 16 + 2 * Sh::IDX_BUF;
+  // per stage: a "full" barrier (the chunk's bulk copies landed) and an
+  // "empty" barrier (every warp is done with the buffer)
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem);
+  uint64_t *empty = full + kGatherStages;
+  unsigned char *const idx0 = smem + Sh::HEAD;
+  unsigned char *const val0 = smem + Sh::HEAD + kGatherStages * Sh::IDX_BUF;
   unsigned short *wlist = reinterpret_cast<unsigned short *>(
-      smem + 16 + 2 * Sh::IDX_BUF + 2 * Sh::VAL_BUF) + (threadIdx.x >> 5) * K;
-  float *g1 = reinterpret_cast<float *>(smem + 16 + 2 * Sh::IDX_BUF + 2 * Sh::VAL_BUF +
+      smem + Sh::HEAD + kGatherStages * (Sh::IDX_BUF + Sh::VAL_BUF)) + (threadIdx.x >> 5) * K;
+  float *g1 = reinterpret_cast<float *>(smem + Sh::HEAD + kGatherStages * (Sh::IDX_BUF + Sh::VAL_BUF) +
                                         Sh::LIST_BYTES);
   __shared__ int s_abort;
+  // the bins of the current tile (its own and the 8 around it; empty ranges
+  // for bins off the grid)
+  __shared__ int s_beg[9], s_end[9];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = kGatherThreads / 32;
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int b = 0; b < kGatherStages; ++b) {
+      mbar_init(&full[b], 1);
+      mbar_init(&empty[b], NW);
+    }
     fence_mbar_init();
     s_abort = 0;
   }
   if constexpr (GAUSS) gauss_fill(g1, S, kp.G, kp.sigma, tid, kGatherThreads);
   __syncthreads();
-  uint32_t uses0 = 0, uses1 = 0;
   const int P = kp.P;
+  // One stream of chunks per CTA, through all its tiles and planes: chunk g
+  // of the stream uses buffer g % kGatherStages.  Thread 0 issues up to
+  // kGatherStages - 1 chunks ahead of its own warp, reusing a buffer once
+  // every warp has released it, so the warps of a tile drift apart by up to
+  // that many chunks instead of meeting at a barrier after every chunk.
+  uint32_t consumed = 0;  // chunks this warp has taken from the stream
+  uint32_t issued = 0;    // thread 0: chunks issued
 
   for (int t = blockIdx.x; t < kp.total_tiles; t += gridDim.x) {
     // tiles of the launch's jobs are numbered from tile_base[0]
@@ -96,6 +118,27 @@ __global__ void __launch_bounds__(kGatherThreads)
     const int tx = lt % ntx, ty = lt / ntx;
     const int x0 = tx * TT, y0 = ty * TT;
     const int cx = x0 + lane, cy0 = y0 + 4 * warp;
+    __syncthreads();  // every warp is done with the previous tile's bin ranges
+    // a timed-out wait anywhere ends the CTA's work: read by every thread
+    // after the barrier (where it was set before), so all leave together
+    if (s_abort) break;
+    if (tid < 9) {
+      const int by = ty - 1 + tid / 3, bx = tx - 1 + tid % 3;
+      int b0 = 0, b1 = 0;
+      if (by >= 0 && by < ntx && bx >= 0 && bx < ntx) {
+        b0 = __ldg(J.bookmarks + by * ntx + bx);
+        b1 = __ldg(J.bookmarks + by * ntx + bx + 1);
+      }
+      s_beg[tid] = b0;
+      s_end[tid] = b1;
+    }
+    __syncthreads();
+    int nch[9], nchunks = 0;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+      nch[q] = (s_end[q] - s_beg[q] + K - 1) / K;
+      nchunks += nch[q];
+    }
     GcfSrc<S, GAUSS, VT> gsrc;
     if constexpr (GAUSS) {
       gsrc.g1 = g1;
@@ -108,6 +151,16 @@ __global__ void __launch_bounds__(kGatherThreads)
     // float load and one packed fused multiply-add
     const float *const greal =
         F32 && !GAUSS && J.gcf_real && J.gcf_imag && *J.gcf_imag == 0 ? J.gcf_real : nullptr;
+    // chunk c of this (tile, plane): bin q and its first record
+    auto chunk_at = [&](int c, int &s0, int &m) {
+      int q = 0;
+      while (q < 8 && c >= nch[q]) {
+        c -= nch[q];
+        ++q;
+      }
+      s0 = s_beg[q] + c * K;
+      m = min(K, s_end[q] - s0);
+    };
     for (int p = 0; p < P; ++p) {
       const VT2 *vplane = reinterpret_cast<const VT2 *>(J.vals) + (size_t)p * J.vstride;
       ACC acc[4];                          // FP64 values
@@ -132,37 +185,43 @@ __global__ void __launch_bounds__(kGatherThreads)
         }
         since = 0;
       };
-      for (int by = max(ty - 1, 0); by <= min(ty + 1, ntx - 1); ++by)
-        for (int bx = max(tx - 1, 0); bx <= min(tx + 1, ntx - 1); ++bx) {
-          const int bin = by * ntx + bx;
-          const int s_beg = __ldg(J.bookmarks + bin), s_end = __ldg(J.bookmarks + bin + 1);
-          const int nchunks = (s_end - s_beg + K - 1) / K;
-          auto issue = [&](int c, int b) {
-            int s0 = s_beg + c * K, e0 = min(s_end, s0 + K);
-            size_t i0 = (size_t)s0 * 8, i1 = (size_t)e0 * 8;
-            size_t v0 = (size_t)s0 * sizeof(VT2), v1 = (size_t)e0 * sizeof(VT2);
-            uint32_t bytes = (uint32_t)(((i1 + 15) & ~(size_t)15) - (i0 & ~(size_t)15)) +
-                             (uint32_t)(((v1 + 15) & ~(size_t)15) - (v0 & ~(size_t)15));
-            fence_proxy_async();
-            mbar_expect_tx(&bar[b], bytes);
-            stage_span((idx0 + b * Sh::IDX_BUF), reinterpret_cast<const char *>(J.idx), i0, i1, &bar[b]);
-            stage_span((val0 + b * Sh::VAL_BUF), reinterpret_cast<const char *>(vplane), v0, v1, &bar[b]);
-          };
-          if (tid == 0 && nchunks > 0) {
-            issue(0, 0);
-            if (nchunks > 1) issue(1, 1);
+      // thread 0: chunk c of this (tile, plane) into the stream, once every
+      // warp has released the buffer it takes
+      auto issue = [&](int c) {
+        const int b = issued % kGatherStages;
+        if (issued >= (uint32_t)kGatherStages &&
+            !mbar_wait(&empty[b], (issued / kGatherStages - 1) & 1, kp.flags)) {
+          s_abort = 1;
+          return false;
+        }
+        int s0, m;
+        chunk_at(c, s0, m);
+        const size_t i0 = (size_t)s0 * 8, i1 = (size_t)(s0 + m) * 8;
+        const size_t v0 = (size_t)s0 * sizeof(VT2), v1 = (size_t)(s0 + m) * sizeof(VT2);
+        const uint32_t bytes = (uint32_t)(((i1 + 15) & ~(size_t)15) - (i0 & ~(size_t)15)) +
+                               (uint32_t)(((v1 + 15) & ~(size_t)15) - (v0 & ~(size_t)15));
+        fence_proxy_async();
+        mbar_expect_tx(&full[b], bytes);
+        stage_span(idx0 + b * Sh::IDX_BUF, reinterpret_cast<const char *>(J.idx), i0, i1, &full[b]);
+        stage_span(val0 + b * Sh::VAL_BUF, reinterpret_cast<const char *>(vplane), v0, v1, &full[b]);
+        ++issued;
+        return true;
+      };
+      int nissued = 0;  // thread 0: chunks of this (tile, plane) issued
+      for (int c = 0; c < nchunks; ++c) {
+        if (tid == 0)
+          while (nissued < nchunks && nissued < c + kGatherStages && !s_abort) {
+            if (!issue(nissued)) break;
+            ++nissued;
           }
-          for (int c = 0; c < nchunks; ++c) {
-            const int b = c & 1;
-            const uint32_t parity = (b == 0 ? uses0 : uses1) & 1;
-            if (!mbar_wait(&bar[b], parity, kp.flags)) s_abort = 1;
-            if (b == 0) ++uses0; else ++uses1;
-            __syncthreads();
-            if (s_abort) break;
-            const int s0 = s_beg + c * K;
-            const int m = min(K, s_end - s0);
-            const int2 *ib = reinterpret_cast<const int2 *>((idx0 + b * Sh::IDX_BUF) + (((size_t)s0 * 8) & 15));
-            const VT2 *vb = reinterpret_cast<const VT2 *>((val0 + b * Sh::VAL_BUF) + (((size_t)s0 * sizeof(VT2)) & 15));
+        const int b = consumed % kGatherStages;
+        if (!mbar_wait(&full[b], (consumed / kGatherStages) & 1, kp.flags)) s_abort = 1;
+        ++consumed;
+        if (s_abort) break;
+        int s0, m;
+        chunk_at(c, s0, m);
+        const int2 *ib = reinterpret_cast<const int2 *>((idx0 + b * Sh::IDX_BUF) + (((size_t)s0 * 8) & 15));
+        const VT2 *vb = reinterpret_cast<const VT2 *>((val0 + b * Sh::VAL_BUF) + (((size_t)s0 * sizeof(VT2)) & 15));
             // this warp's records: footprint (columns mx-H+1 .. mx+H, rows
             // my-H+1 .. my+H) overlapping the tile's columns and the warp's
             // rows cy0 .. cy0+3, in chunk order
@@ -243,13 +302,10 @@ __global__ void __launch_bounds__(kGatherThreads)
                 }
               }
             }
-            __syncthreads();  // buffer b consumed by every warp
-            if (tid == 0 && c + 2 < nchunks) issue(c + 2, b);
-          }
-          if (s_abort) by = ntx;  // leave both bin loops
-          if (s_abort) break;
-        }
-      if (s_abort) break;
+            __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[b]);  // this warp is done with buffer b
+      }
+      if (s_abort) break;  // on to the next tile's barrier, where the CTA stops
       if constexpr (F32) merge_runs();
       // each cell written once: plain stores, coalesced along x
       const size_t NN = (size_t)N * N;
@@ -287,12 +343,12 @@ __global__ void __launch_bounds__(kGatherThreads)
         }
       }
     }
-    if (s_abort) break;
   }
-  if (s_abort && tid == 0) {
-    mbar_wait(&bar[0], uses0 & 1, nullptr);
-    mbar_wait(&bar[1], uses1 & 1, nullptr);
-  }
+  // A timed-out wait may leave bulk copies in flight: thread 0 waits
+  // (bounded) for the chunks it issued before the CTA's shared memory goes.
+  if (s_abort && tid == 0)
+    for (uint32_t g = issued > (uint32_t)kGatherStages ? issued - kGatherStages : 0; g < issued; ++g)
+      mbar_wait(&full[g % kGatherStages], (g / kGatherStages) & 1, nullptr);
 }
 
 template <int S, class ACC, bool GAUSS>
