@@ -313,8 +313,12 @@ int gg_bin(gg_context *ctx, const gg_options *opt, int uv_type, const void *uv,
  * order while the HBM budget allows (grid + staged inputs + workspace share);
  * whenever a slot is free, every admitted request not yet started is
  * gridded in one batched launch there, so requests that arrive while others
- * are on the GPU overlap with them on the device.  Latency = arrival to
- * grid ready on the host side of the stream. */
+ * are on the GPU overlap with them on the device.  Host inputs are copied in
+ * on one server-wide input stream and grids copied out on one server-wide
+ * output stream, ordered with the slot's kernels by events: a slot takes its
+ * next batch as soon as its kernels finish, while earlier grids are still
+ * being copied out.  Requests complete in launch order.  Latency = arrival
+ * to grid ready (in host memory for host-bound requests). */
 typedef struct gg_server gg_server;
 
 #define GG_SERVER_TUNE_BATCHES 32
